@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""f-fdot cells/s of the Fourier-domain acceleration search on one GB300.
+
+One "step" = one whole batched search over a fixed synthetic batch of DM
+trials (the batched configuration: trial lengths uniform in
+{2^20, 2^21, 2^22, 3*2^20} samples at dt = 64 us, 10% with one injected
+accelerated sinusoid, zmax = 200, 8 harmonics, 8192-point segments):
+R2C FFT, whitening, every overlap-save step of every trial (segment
+preparation, fused correlation / inverse FFT / power plane, harmonic sum
+and threshold) and the read-back of the candidate list.
+
+    value   cells/s with the series already in HBM when timing starts
+    e2e     the same through the C ABI from pinned host buffers (host->device
+            copy of every series and device->host read of the candidates
+            inside the timed region)
+
+A cell is one fundamental f-fdot point (r step 1/2, z step 2) carried
+through all harmonic stages.  --impl reference times the CPU oracle (a
+restatement of the reference pipeline, FP64) on a bounded sample instead.
+Under torchrun every rank searches its own trials (no collective); rank 0
+prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LENGTHS = [1 << 20, 1 << 21, 1 << 22, 3 << 20]
+DT = 64e-6
+ZMAX, NUMHARM, FFTLEN = 200, 8, 8192
+METRIC = "f-fdot cells/s (zmax=200, 8 harmonics, batched)"
+# algorithmic HBM bytes per fundamental cell at zmax=200 / 8 harmonics:
+# every harmonic plane written once (4 B) and read once (4 B) per cell of
+# that plane; the planes hold 3.205x the fundamental cells.
+PLANE_RATIO = None  # computed from the bank geometry
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--trials", type=int, default=256, help="DM trials per GPU")
+    ap.add_argument("--chunk", type=int, default=0, help="segments per launch group (0: auto)")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 8:
+                    rows.append(p)
+        os.unlink(self.f.name)
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- workload
+def make_batch(ntrials: int, seed: int):
+    """Seeded trial lengths and signals (host description)."""
+    rng = np.random.default_rng(seed)
+    lengths = [int(x) for x in rng.choice(LENGTHS, ntrials)]
+    sigs = []
+    for n in lengths:
+        if rng.random() < 0.10:
+            sigs.append((float(rng.uniform(0.02, 0.1)), float(rng.uniform(1e4, min(1e6, 0.4 * n))),
+                         float(rng.uniform(-150, 150))))
+        else:
+            sigs.append(None)
+    return lengths, sigs
+
+
+def device_series(torch, lengths, sigs, seed):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    out = []
+    for n, s in zip(lengths, sigs):
+        x = torch.randn(n, generator=g, device="cuda", dtype=torch.float32)
+        if s is not None:
+            amp, r0, z = s
+            t = torch.arange(n, device="cuda", dtype=torch.float64) / n
+            x += (amp * torch.cos(2 * np.pi * (r0 * t + 0.5 * z * t * t))).float()
+        out.append(x)
+    return out
+
+
+# ------------------------------------------------------------ cpu baseline
+def cpu_baseline(seconds: float):
+    """The oracle (FP64 restatement of the reference path) on a bounded
+    sample: overlap-save steps of one 2^22-sample trial, all host threads."""
+    from gpu_accelsearch_gb300.synth import synth_series
+    from oracle import oracle as O
+    n = 1 << 22
+    x = synth_series(n, seed=1, signals=[(0.05, 200000.25, 40.0)])
+    spec = np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2]
+    w = O.deredden(spec)
+    U = 7734
+    orc = O.Oracle(ZMAX, NUMHARM, U)
+    cores = os.cpu_count() or 1
+    cuts = np.array([O.power_cut(6.0, 1 << s) for s in range(orc.nstages)])
+    rlo = int(np.floor(np.float32(n) * np.float32(DT)))
+    t = time.perf_counter()
+    orc.run_steps(w, rlo, 0, 1, powcut=cuts, cap=1 << 16, nthreads=cores)
+    t1 = time.perf_counter() - t
+    nsteps = int(max(1, min(541, seconds / max(t1, 1e-3))))
+    t = time.perf_counter()
+    orc.run_steps(w, rlo, 1, nsteps, powcut=cuts, cap=1 << 16, nthreads=cores)
+    el = time.perf_counter() - t
+    cells = nsteps * U * int(orc.geom[0, 3])
+    orc.close()
+    return {"value": cells / el, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": f"{nsteps} overlap-save steps of one 2^22-sample trial (zmax=200, 8 "
+                      f"harmonics, L=8192, uselen=7734): FP64 oracle planes + harmonic sum + "
+                      f"threshold, {el:.1f} s"}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    per = max(1.0, args.cpu_seconds / 3)
+    for _ in range(args.warmup):
+        cpu_baseline(per / 4)
+    vals = [cpu_baseline(per)["value"] for _ in range(args.steps)]
+    cb = cpu_baseline(per)
+    v = float(np.median(vals))
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded N(0,1) float32 series with an injected sinusoid",
+            "impl": "reference",
+            "config": {"workload": "bounded sample of the batched configuration on the host: "
+                                   "overlap-save steps of one 2^22-sample trial, zmax=200, "
+                                   "8 harmonics, L=8192",
+                       "implementation": "CPU oracle port of the reference pipeline "
+                                         "(oracle/accel_oracle.c), OpenMP over templates"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    """DRAM bytes per segment of the plane kernel from the committed ncu
+    summary (profiles/plane_kernel_traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "plane_kernel_traffic.json")) as f:
+            return float(json.load(f)["dram_bytes_per_segment"])
+    except Exception:
+        return None
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, local, world = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from gpu_accelsearch_gb300.search import AccelSearch
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    lengths, sigs = make_batch(args.trials, seed=1000 + rank)
+    series = device_series(torch, lengths, sigs, seed=2000 + rank)
+    ptrs = [x.data_ptr() for x in series]
+    s = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=args.chunk,
+                    device=local)
+    U, nz0 = s.uselen, s.harmonics[0].numzs
+    nseg = sum(s.step_count(n, DT) for n in lengths)
+    cells = nseg * U * nz0
+    plane_cells = 0
+    for h in s.harmonics:  # mean row width over the step phases ~ plane_width - 1
+        plane_cells += h.numzs * (U if h.harmnum == h.maxharm == 1 else h.plane_width - 1)
+    bytes_per_cell = 8.0 * plane_cells / (U * nz0)
+
+    for _ in range(args.warmup):
+        s.search(ptrs, DT, on_device=True, nsamples=lengths)
+    torch.cuda.synchronize()
+
+    # ---- value: device-resident inputs
+    s.reset_stats()
+    s.profile(True)
+    clk = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    t0 = time.perf_counter()
+    ncand = 0
+    for _ in range(args.steps):
+        ncand = s.search(ptrs, DT, on_device=True, nsamples=lengths)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    clocks = clk.stop()
+    barrier()
+    st = s.stats()
+    s.profile(False)
+    el_t = torch.tensor([el], device="cuda")
+    if world > 1:
+        dist.all_reduce(el_t, op=dist.ReduceOp.MAX)
+    el = float(el_t.item())
+    value = cells * args.steps * world / el
+
+    # ---- e2e: pinned host series through the C ABI
+    e2e = None
+    if not args.no_e2e:
+        host = [x.cpu().pin_memory() for x in series]
+        hptrs = [h.data_ptr() for h in host]
+        s.search_ptrs(hptrs, lengths, DT, on_device=False)  # warm
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nc = 0
+        for _ in range(args.steps):
+            nc = s.search_ptrs(hptrs, lengths, DT, on_device=False)
+        torch.cuda.synchronize()
+        el2 = time.perf_counter() - t0
+        barrier()
+        el2_t = torch.tensor([el2], device="cuda")
+        if world > 1:
+            dist.all_reduce(el2_t, op=dist.ReduceOp.MAX)
+        e2e = {"value": cells * args.steps * world / float(el2_t.item()), "unit": "cells/s",
+               "h2d_bytes_per_step": int(sum(lengths) * 4),
+               "d2h_bytes_per_step": int(8 + 16 * nc)}
+
+    # ---- plain per-trial path: one 2^22 trial, one step per launch group
+    plain = None
+    if not args.no_plain and rank == 0:
+        p = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=1, device=local)
+        xs = device_series(torch, [1 << 22], [None], seed=7)
+        pn = p.step_count(1 << 22, DT)
+        p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
+        torch.cuda.synchronize()
+        pel = time.perf_counter() - t0
+        plain = {"value": pn * U * nz0 * reps / pel, "unit": "cells/s",
+                 "workload": "one 2^22-sample trial, one overlap-save step per launch group "
+                             f"({pn} steps)"}
+        p.close()
+
+    if rank != 0:
+        s.close()
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_kind = load_peaks()
+    k = st["kinds"]
+    plane_ms = k["plane"]["ms"]
+    plane_launches = max(k["plane"]["launches"], 1)
+    seg_per_launch = st["segments"] / max(k["hsum"]["launches"], 1)
+    # algorithmic bytes of the plane kernel: each plane cell written once (4 B)
+    plane_bytes = 0.5 * bytes_per_cell * st["cells"]
+    achieved = plane_bytes / (plane_ms / 1e3) / 1e9 if plane_ms > 0 else None
+    tr = load_traffic()
+    roofline = {"bound": "hbm", "kernel": "k_plane (fused correlate + inverse FFT + |X|^2)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None,
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_cell": 0.5 * bytes_per_cell,
+                "traffic": (tr * st["segments"] / plane_launches) if tr else None,
+                "note": "achieved = 4 B per plane cell written / CUDA-event time of the "
+                        "plane launches in the timed region"}
+    step_roofline = {"bytes_per_cell": bytes_per_cell, "achieved": value * bytes_per_cell / 1e9,
+                     "peak": peak, "unit": "GB/s", "frac": value * bytes_per_cell / 1e9 / peak}
+    kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                   "share": round(v["ms"] / max(sum(x["ms"] for x in k.values()), 1e-9), 4)}
+            for name, v in k.items()}
+    cb = cpu_baseline(args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded N(0,1) float32 series (torch Philox), 10% with one "
+                "injected accelerated sinusoid",
+        "config": {"workload": f"batched: {args.trials} DM trials per GPU, lengths uniform in "
+                               "{2^20, 2^21, 2^22, 3*2^20}, dt=64us, zmax=200, 8 harmonics, "
+                               f"L=8192 (uselen {U}), sigma=6",
+                   "segments_per_step": nseg, "cells_per_step": cells,
+                   "chunk_segments": s.config.chunk_segments or "auto",
+                   "l2": f"inputs ({sum(lengths) * 4 / 1e9:.2f} GB of series per GPU) larger "
+                         "than L2; no flush",
+                   "parallelism": f"trial-sharded replicas x{world}"},
+        "roofline": roofline, "step_roofline": step_roofline, "kernels": kern,
+        "cpu_baseline": cb, "e2e": e2e, "gpu_launches": st["launches"], "clocks": clocks,
+        "plain": plain,
+        "batched_over_plain": (value / world / plain["value"]) if plain else None,
+        "candidates_per_step": ncand,
+    }
+    print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

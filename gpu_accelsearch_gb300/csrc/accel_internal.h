@@ -1,0 +1,115 @@
+// accel_internal.h -- types shared by the CUDA translation units of
+// libaccelsearch.so.  Nothing here is part of the public C ABI
+// (include/accelsearch.h).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "accel_common.cuh"
+
+namespace accel {
+
+// One harmonic of a template bank, as the kernels see it.
+struct BankHarmDev {
+    int harmnum, maxharm;   // fraction harmnum/maxharm of the fundamental
+    int zmax;               // largest |z| of this harmonic's templates
+    int numzs;              // templates, z = -zmax + 2 j
+    int M;                  // half segment length (L = 2M)
+    int hw0;                // halfwidth of the widest template (z = -zmax)
+    int zlo;                // calc_required_z(f, -zmax_full)
+    int tpl_base;           // first template index of this harmonic in the bank
+    float2* kstd;           // [numzs][L]  FFT_L of the wrapped template
+    float2* fold;           // [numzs][2M] A | B (see bank.cu)
+    __half2* fold16;        // [numzs][2M] fold / scale, or null
+    float* fold16_scale;    // [numzs]
+};
+
+// Per-segment descriptor: which whitened spectrum and where the step starts.
+struct SegDesc {
+    const float2* spec;     // whitened spectrum (bins [0, numbins) valid)
+    long long numbins;      // N/2
+    long long startr;       // first fundamental bin of the step
+    int trial;              // caller's trial index
+    int step;               // step index within the trial
+};
+
+// Per-harmonic plan of a search: bank data plus plane layout.
+struct HarmPlan {
+    int p, q;               // harmnum, maxharm
+    int M;                  // half segment length
+    int hw0, zlo, numzs;
+    int wmax;               // columns written per f-dot row (max numrs over steps)
+    int prow;               // row stride of the power plane (floats, multiple of 4)
+    long long poff;         // offset of this plane inside a segment's plane block (floats)
+    long long doff;         // offset of this harmonic's segment spectrum (float2)
+    int zbase;              // prefix of numzs within the harmonic's M class
+    const float2* fold;
+    const __half2* fold16;
+    const float* f16scale;
+};
+
+struct PrepArgs {
+    HarmPlan h[kMaxHarm];
+    int nh;                 // harmonics in this launch (one M class)
+    int uselen;
+    const SegDesc* segs;
+    float2* dbuf;           // [nseg][dstride]
+    long long dstride;
+};
+
+struct PlaneArgs {
+    HarmPlan h[kMaxHarm];
+    int nh;                 // harmonics in this launch (one M class)
+    int ntpl;               // sum of numzs over them
+    const float2* dbuf;
+    long long dstride;
+    float* planes;          // [nseg][pstride]
+    long long pstride;
+    int use_fp16;
+};
+
+// Raw candidate as written by the harmonic-sum kernel (16 bytes).
+struct RawCand {
+    int32_t seg;            // segment index within the launch group
+    int32_t ridx;           // fundamental r index, r = startr + ridx / 2
+    int16_t zidx;           // fundamental z index, z = zlo0 + 2 zidx
+    int16_t numharm;        // harmonics summed
+    float power;
+};
+
+struct HsumArgs {
+    HarmPlan h[kMaxHarm];
+    int nh;                 // all harmonics of the bank, bank order
+    int uselen;
+    int numzs0, zlo0;
+    int stage_of[kMaxHarm]; // stage index after harmonic h, or -1
+    float cut[kMaxStages];
+    const SegDesc* segs;
+    const float* planes;
+    long long pstride;
+    RawCand* cands;
+    unsigned long long* ncand;
+    long long cap;
+    int seg_base;           // added to the segment index stored in candidates
+    float* stage_out;       // optional [nseg][nstages][numzs0][uselen]
+    int nstages;
+};
+
+// ---- launchers (return 0 or -1 after a launch error) ----
+int launch_twiddles(float2* tw, cudaStream_t st);
+int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int nh, int ntpl,
+                      float2* resp, int rstride, bool fp16, cudaStream_t st);
+int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);
+int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
+int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
+
+// whitening
+struct WhitenPlan;
+int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
+                  unsigned numbins, int maxlen, cudaStream_t st);
+
+}  // namespace accel

@@ -1,0 +1,934 @@
+// api.cu -- host side of libaccelsearch.so: the accel_* C ABI, the search
+// context (template bank, plans, work buffers) and the overlap-save driver.
+//
+// The reference drives one DM trial from main() (AccelSearch.cu:48-281): a
+// host loop over steps, each step a synchronous H2D copy of host-prepared
+// segments and a sequence of launches.  Here a search call takes any number
+// of trials, keeps their spectra on the device, and runs the steps of all
+// of them in launch groups of `chunk` segments: segment preparation, the
+// fused plane kernel and the harmonic sum, with no host round trip.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/accelsearch.h"
+#include "accel_internal.h"
+
+using namespace accel;
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                    \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess)                                                                   \
+            return set_err(ACCEL_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));         \
+    } while (0)
+
+#define CKL(x, what)                                                                             \
+    do {                                                                                         \
+        if ((x) != 0) {                                                                          \
+            cudaError_t e_ = cudaGetLastError();                                                 \
+            return set_err(ACCEL_ERR_CUDA, "%s launch failed: %s", what, cudaGetErrorString(e_)); \
+        }                                                                                        \
+    } while (0)
+
+// ---- Gamma(n,1) tail and Gaussian equivalents (candidate cut and sigma)
+double log_gamma_q(int n, double x) {  // log P(Gamma(n,1) > x)
+    double term = 1.0, s = 1.0;
+    for (int k = 1; k < n; k++) {
+        term *= x / k;
+        s += term;
+    }
+    return -x + std::log(s);
+}
+double log_gauss_tail(double sigma) {  // log P(N(0,1) > sigma)
+    if (sigma < 30.0) return std::log(0.5 * std::erfc(sigma / std::sqrt(2.0)));
+    // asymptotic expansion beyond double erfc's range
+    double s2 = sigma * sigma;
+    return -0.5 * s2 - std::log(sigma * std::sqrt(2.0 * M_PI)) + std::log1p(-1.0 / s2 + 3.0 / (s2 * s2));
+}
+double power_cut(double sigma, int numharm, double numindep) {
+    double logp = log_gauss_tail(sigma) - std::log(numindep > 1.0 ? numindep : 1.0);
+    double lo = 0.0, hi = 4096.0;
+    for (int it = 0; it < 200; it++) {
+        double mid = 0.5 * (lo + hi);
+        if (log_gamma_q(numharm, mid) > logp) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+double sigma_of_power(double power, int numharm, double numindep) {
+    double logp = log_gamma_q(numharm, power) + std::log(numindep > 1.0 ? numindep : 1.0);
+    if (logp >= std::log(0.5)) return 0.0;
+    double lo = 0.0, hi = 200.0;
+    for (int it = 0; it < 200; it++) {
+        double mid = 0.5 * (lo + hi);
+        if (log_gauss_tail(mid) > logp) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+struct WhitenPlanDev {
+    int nb = 0, maxlen = 0;
+    int* d_start = nullptr;
+    int* d_len = nullptr;
+    double* d_med = nullptr;
+};
+
+// Serial block recurrence of deredden (bpd_noise.c:33-79).
+std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbuf, int maxbuf) {
+    std::vector<std::pair<int, int>> b;
+    int binnum = 1, buflen = initbuf;
+    b.push_back({binnum, buflen});
+    binnum += buflen;
+    buflen = (int)(initbuf * std::log((double)binnum));
+    if (buflen > maxbuf) buflen = maxbuf;
+    while ((unsigned)(binnum + buflen) < numbins) {
+        b.push_back({binnum, buflen});
+        binnum += buflen;
+        buflen = (int)(initbuf * std::log((double)binnum));
+        if (buflen > maxbuf) buflen = maxbuf;
+    }
+    return b;
+}
+
+struct TrialBuf {
+    long long n = 0;
+    float* series = nullptr;
+    float2* spec = nullptr;
+};
+
+}  // namespace
+
+struct accel_ctx {
+    accel_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int uselen = 0, nh = 0, nstages = 0, numzs0 = 0, zlo0 = 0;
+
+    // bank
+    BankHarmDev bh[kMaxHarm]{};
+    BankHarmDev* d_bh = nullptr;
+    void* bank_mem = nullptr;
+    int ntpl = 0;
+    float2* tw = nullptr;
+
+    // plan
+    HarmPlan hp[kMaxHarm]{};
+    int stage_of[kMaxHarm]{};
+    std::vector<int> mvals;
+    long long dstride = 0, pstride = 0;
+    float cuts[kMaxStages]{};
+
+    // work buffers
+    int chunk = 1;
+    float2* dbuf = nullptr;
+    float* planes = nullptr;
+    SegDesc* d_segs = nullptr;
+    SegDesc* h_segs = nullptr;  // pinned
+    long long segs_cap = 0;
+    RawCand* d_cands = nullptr;
+    unsigned long long* d_ncand = nullptr;
+    unsigned long long* h_ncand = nullptr;  // pinned
+    long long cand_cap = 0;
+
+    std::map<unsigned, WhitenPlanDev> wplans;
+    std::map<long long, cufftHandle> fftplans;
+    std::vector<TrialBuf> trials;
+
+    std::vector<accel_candidate> results;
+    unsigned long long last_raw = 0;
+
+    // accounting
+    bool profiling = false;
+    struct Ev { int kind; cudaEvent_t a, b; };
+    std::vector<Ev> pending;
+    std::vector<cudaEvent_t> evpool;
+    accel_stats stats{};
+};
+
+namespace {
+
+int ensure_device(accel_ctx* c) {
+    CK(cudaSetDevice(c->device));
+    return ACCEL_OK;
+}
+
+enum { K_PREP = 0, K_PLANE = 1, K_HSUM = 2, K_WHITEN = 3, K_RFFT = 4 };
+
+cudaEvent_t take_event(accel_ctx* c) {
+    cudaEvent_t e = nullptr;
+    if (!c->evpool.empty()) {
+        e = c->evpool.back();
+        c->evpool.pop_back();
+    } else {
+        cudaEventCreate(&e);
+    }
+    return e;
+}
+
+// Bracket `nlaunch` kernel launches of one kind with events (when profiling).
+struct ProfScope {
+    accel_ctx* c;
+    int kind;
+    cudaEvent_t a = nullptr;
+    ProfScope(accel_ctx* c_, int kind_, int nlaunch) : c(c_), kind(kind_) {
+        if (kind != K_RFFT) c->stats.launches += nlaunch;
+        c->stats.kind_launches[kind] += nlaunch;
+        if (c->profiling) {
+            a = take_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = take_event(c);
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({kind, a, b});
+        }
+    }
+};
+
+// Fold finished event pairs into the stats (the stream must be idle).
+void prof_collect(accel_ctx* c) {
+    for (auto& e : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) c->stats.kind_ms[e.kind] += ms;
+        c->evpool.push_back(e.a);
+        c->evpool.push_back(e.b);
+    }
+    c->pending.clear();
+}
+
+int build_bank(accel_ctx* c) {
+    int info_zmax = c->cfg.zmax, numharm = c->cfg.numharm, U = c->uselen;
+    // bank order: stage by stage, odd harmonics (bpd_subharmonics.cu:319-354)
+    int stages = 0;
+    while ((1 << stages) < numharm) stages++;
+    stages += 1;
+    int n = 0, tb = 0, rmax = 0;
+    size_t bytes = 0;
+    for (int st = 0; st < stages; st++) {
+        int maxh = st < 1 ? 1 : (1 << st);
+        for (int h = 1; h <= maxh; h += 2) {
+            BankHarmDev& b = c->bh[n];
+            b.harmnum = h;
+            b.maxharm = maxh;
+            b.zmax = required_z(h, maxh, info_zmax);
+            b.numzs = (b.zmax / kDz) * 2 + 1;
+            int hwz = z_halfwidth((double)required_z(h, maxh, info_zmax));
+            long long L = next_pow2((long long)(U * h) / maxh + 2 + 2 * kNumBetween * hwz);
+            if (L < 2 * kMinM || L > 2 * kMaxM)
+                return set_err(ACCEL_ERR_UNSUPPORTED,
+                               "harmonic %d/%d needs an FFT of %lld points; supported 128..16384", h,
+                               maxh, L);
+            b.M = (int)(L / 2);
+            b.hw0 = z_halfwidth((double)(-b.zmax));
+            b.zlo = required_z(h, maxh, -info_zmax);
+            b.tpl_base = tb;
+            tb += b.numzs;
+            int hwmax = b.hw0;
+            rmax = std::max(rmax, 4 * hwmax);
+            bytes += (size_t)b.numzs * L * sizeof(float2) * 2;  // kstd + fold
+            if (c->cfg.template_fp16) bytes += (size_t)b.numzs * L * sizeof(__half2) + b.numzs * sizeof(float);
+            bytes = (bytes + 255) & ~(size_t)255;
+            n++;
+        }
+    }
+    c->nh = n;
+    c->ntpl = tb;
+    c->nstages = stages;
+    CK(cudaMalloc(&c->bank_mem, bytes));
+    char* p = (char*)c->bank_mem;
+    for (int h = 0; h < n; h++) {
+        BankHarmDev& b = c->bh[h];
+        size_t L = 2 * (size_t)b.M;
+        b.kstd = (float2*)p;
+        p += b.numzs * L * sizeof(float2);
+        b.fold = (float2*)p;
+        p += b.numzs * L * sizeof(float2);
+        if (c->cfg.template_fp16) {
+            b.fold16 = (__half2*)p;
+            p += b.numzs * L * sizeof(__half2);
+            b.fold16_scale = (float*)p;
+            p += b.numzs * sizeof(float);
+        }
+        p = (char*)c->bank_mem + ((p - (char*)c->bank_mem + 255) & ~(size_t)255);
+    }
+    CK(cudaMalloc(&c->d_bh, sizeof(BankHarmDev) * n));
+    CK(cudaMemcpyAsync(c->d_bh, c->bh, sizeof(BankHarmDev) * n, cudaMemcpyHostToDevice, c->stream));
+    float2* resp = nullptr;
+    CK(cudaMalloc(&resp, sizeof(float2) * (size_t)tb * rmax));
+    CK(cudaMemsetAsync(resp, 0, sizeof(float2) * (size_t)tb * rmax, c->stream));
+    CKL(launch_bank_build(c->d_bh, c->bh, n, tb, resp, rmax, c->cfg.template_fp16 != 0, c->stream),
+        "template bank");
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaFree(resp));
+    return ACCEL_OK;
+}
+
+int build_plan(accel_ctx* c) {
+    const int U = c->uselen;
+    long long doff = 0, poff = 0;
+    int stage = 0;
+    for (int h = 0; h < c->nh; h++) {
+        const BankHarmDev& b = c->bh[h];
+        HarmPlan& P = c->hp[h];
+        P.p = b.harmnum;
+        P.q = b.maxharm;
+        P.M = b.M;
+        P.hw0 = b.hw0;
+        P.zlo = b.zlo;
+        P.numzs = b.numzs;
+        P.fold = b.fold;
+        P.fold16 = b.fold16;
+        P.f16scale = b.fold16_scale;
+        // widest window over all step phases (the geometry repeats with period q in startr)
+        int wmax = 0;
+        for (long long s = 0; s < 4LL * P.q; s++) {
+            StepHarm g = step_harm(1000000 + s, U, P.p, P.q, P.hw0);
+            wmax = std::max(wmax, g.numrs);
+            if (next_pow2(g.numdata) != P.M)
+                return set_err(ACCEL_ERR_INVALID,
+                               "harmonic %d/%d: segment of %d bins does not fit half length %d", P.p,
+                               P.q, g.numdata, P.M);
+        }
+        if (P.hw0 + wmax / 2 > P.M)
+            return set_err(ACCEL_ERR_INVALID, "harmonic %d/%d: window exceeds segment", P.p, P.q);
+        P.wmax = wmax;
+        P.prow = (wmax + 3) & ~3;
+        P.poff = poff;
+        poff += (long long)P.prow * P.numzs;
+        P.doff = doff;
+        doff += P.M;
+        c->stage_of[h] = (((h + 1) & h) == 0) ? stage++ : -1;
+    }
+    c->dstride = (doff + 31) & ~31LL;
+    c->pstride = (poff + 63) & ~63LL;
+    c->numzs0 = c->hp[0].numzs;
+    c->zlo0 = c->hp[0].zlo;
+    // zind must stay inside each harmonic's plane for every fundamental row
+    for (int h = 1; h < c->nh; h++) {
+        for (int z = 0; z < c->numzs0; z++) {
+            int zi = sub_zind(c->zlo0 + kDz * z, c->hp[h].p, c->hp[h].q, c->hp[h].zlo);
+            if (zi < 0 || zi >= c->hp[h].numzs)
+                return set_err(ACCEL_ERR_INVALID, "f-dot index out of range for harmonic %d", h);
+        }
+    }
+    c->mvals.clear();
+    for (int h = 0; h < c->nh; h++)
+        if (std::find(c->mvals.begin(), c->mvals.end(), c->hp[h].M) == c->mvals.end())
+            c->mvals.push_back(c->hp[h].M);
+    for (int s = 0; s < c->nstages; s++)
+        c->cuts[s] = (float)power_cut(c->cfg.sigma, 1 << s, c->cfg.numindep);
+    return ACCEL_OK;
+}
+
+int alloc_work(accel_ctx* c) {
+    long long plane_bytes = c->pstride * 4;
+    int chunk = c->cfg.chunk_segments;
+    if (chunk <= 0) {
+        chunk = (int)std::max(1LL, std::min(256LL, (2LL << 30) / plane_bytes));
+    }
+    c->chunk = chunk;
+    CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * chunk));
+    CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * chunk));
+    c->cand_cap = c->cfg.cand_capacity > 0 ? c->cfg.cand_capacity : (1LL << 22);
+    CK(cudaMalloc(&c->d_cands, sizeof(RawCand) * c->cand_cap));
+    CK(cudaMalloc(&c->d_ncand, sizeof(unsigned long long)));
+    CK(cudaMallocHost(&c->h_ncand, sizeof(unsigned long long)));
+    return ACCEL_OK;
+}
+
+int ensure_segs(accel_ctx* c, long long n) {
+    if (n <= c->segs_cap) return ACCEL_OK;
+    if (c->d_segs) cudaFree(c->d_segs);
+    if (c->h_segs) cudaFreeHost(c->h_segs);
+    c->d_segs = nullptr;
+    c->h_segs = nullptr;
+    long long cap = std::max(n, 2 * c->segs_cap);
+    CK(cudaMalloc(&c->d_segs, sizeof(SegDesc) * cap));
+    CK(cudaMallocHost(&c->h_segs, sizeof(SegDesc) * cap));
+    c->segs_cap = cap;
+    return ACCEL_OK;
+}
+
+int whiten_plan(accel_ctx* c, unsigned numbins, WhitenPlanDev** out) {
+    auto it = c->wplans.find(numbins);
+    if (it != c->wplans.end()) {
+        *out = &it->second;
+        return ACCEL_OK;
+    }
+    if (numbins <= (unsigned)(1 + c->cfg.whiten_initbuf))
+        return set_err(ACCEL_ERR_INVALID, "spectrum of %u bins is too short to whiten", numbins);
+    auto blocks = plan_whiten_blocks(numbins, c->cfg.whiten_initbuf, c->cfg.whiten_maxbuf);
+    WhitenPlanDev w;
+    w.nb = (int)blocks.size();
+    std::vector<int> s(w.nb), l(w.nb);
+    for (int i = 0; i < w.nb; i++) {
+        s[i] = blocks[i].first;
+        l[i] = blocks[i].second;
+        w.maxlen = std::max(w.maxlen, l[i]);
+    }
+    CK(cudaMalloc(&w.d_start, sizeof(int) * w.nb));
+    CK(cudaMalloc(&w.d_len, sizeof(int) * w.nb));
+    CK(cudaMalloc(&w.d_med, sizeof(double) * w.nb));
+    CK(cudaMemcpy(w.d_start, s.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.d_len, l.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice));
+    auto r = c->wplans.emplace(numbins, w);
+    *out = &r.first->second;
+    return ACCEL_OK;
+}
+
+int do_whiten(accel_ctx* c, float2* spec, unsigned numbins) {
+    WhitenPlanDev* w = nullptr;
+    int rc = whiten_plan(c, numbins, &w);
+    if (rc) return rc;
+    ProfScope ps(c, K_WHITEN, 2);
+    CKL(launch_whiten(w->d_start, w->d_len, w->nb, w->d_med, spec, numbins, w->maxlen, c->stream),
+        "whitening");
+    return ACCEL_OK;
+}
+
+int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec) {
+    cufftHandle plan;
+    auto it = c->fftplans.find(n);
+    if (it == c->fftplans.end()) {
+        if (cufftPlan1d(&plan, (int)n, CUFFT_R2C, 1) != CUFFT_SUCCESS)
+            return set_err(ACCEL_ERR_CUDA, "cufftPlan1d(%lld, R2C) failed", n);
+        c->fftplans[n] = plan;
+    } else {
+        plan = it->second;
+    }
+    ProfScope ps(c, K_RFFT, 1);
+    if (cufftSetStream(plan, c->stream) != CUFFT_SUCCESS)
+        return set_err(ACCEL_ERR_CUDA, "cufftSetStream failed");
+    if (cufftExecR2C(plan, const_cast<float*>(series), reinterpret_cast<cufftComplex*>(spec)) !=
+        CUFFT_SUCCESS)
+        return set_err(ACCEL_ERR_CUDA, "cufftExecR2C failed");
+    return ACCEL_OK;
+}
+
+// Launch one group of nseg prepared segment descriptors (device array).
+int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float* stage_out,
+              const float2* dh_in, float* planes_out, bool do_prep, bool do_plane, bool do_sum) {
+    float2* dbuf = dh_in ? const_cast<float2*>(dh_in) : c->dbuf;
+    float* planes = planes_out ? planes_out : c->planes;
+    for (int M : c->mvals) {
+        PrepArgs pa{};
+        PlaneArgs la{};
+        int k = 0, zb = 0;
+        for (int h = 0; h < c->nh; h++) {
+            if (c->hp[h].M != M) continue;
+            pa.h[k] = c->hp[h];
+            la.h[k] = c->hp[h];
+            la.h[k].zbase = zb;
+            zb += c->hp[h].numzs;
+            k++;
+        }
+        pa.nh = k;
+        pa.uselen = c->uselen;
+        pa.segs = d_segs;
+        pa.dbuf = dbuf;
+        pa.dstride = c->dstride;
+        la.nh = k;
+        la.ntpl = zb;
+        la.dbuf = dbuf;
+        la.dstride = c->dstride;
+        la.planes = planes;
+        la.pstride = c->pstride;
+        la.use_fp16 = c->cfg.template_fp16;
+        if (do_prep) {
+            ProfScope ps(c, K_PREP, 1);
+            CKL(launch_prep(M, pa, nseg, c->tw, c->stream), "segment preparation");
+        }
+        if (do_plane) {
+            ProfScope ps(c, K_PLANE, 1);
+            CKL(launch_plane(M, la, nseg, c->tw, c->stream), "power plane");
+        }
+    }
+    if (do_sum) {
+        HsumArgs ha{};
+        for (int h = 0; h < c->nh; h++) {
+            ha.h[h] = c->hp[h];
+            ha.stage_of[h] = c->stage_of[h];
+        }
+        ha.nh = c->nh;
+        ha.uselen = c->uselen;
+        ha.numzs0 = c->numzs0;
+        ha.zlo0 = c->zlo0;
+        for (int s = 0; s < c->nstages; s++) ha.cut[s] = c->cuts[s];
+        ha.segs = d_segs;
+        ha.planes = planes;
+        ha.pstride = c->pstride;
+        ha.cands = c->d_cands;
+        ha.ncand = c->d_ncand;
+        ha.cap = c->cand_cap;
+        ha.seg_base = seg_base;
+        ha.stage_out = stage_out;
+        ha.nstages = c->nstages;
+        ProfScope ps(c, K_HSUM, 1);
+        c->stats.segments += nseg;
+        c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
+        CKL(launch_hsum(ha, nseg, c->stream), "harmonic sum");
+    }
+    return ACCEL_OK;
+}
+
+// Segment table: one entry per (trial, step), trial-major.
+struct SegSpan {
+    std::vector<int> trial, step;
+};
+
+int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* numbins,
+               const long long* rlo) {
+    long long total = 0;
+    const long long half = (unsigned short)(c->uselen / 2);
+    std::vector<long long> nsteps(ntrials);
+    for (int i = 0; i < ntrials; i++) {
+        long long s = 0;
+        for (long long r = rlo[i]; r + half < numbins[i]; r += half) s++;
+        nsteps[i] = s;
+        total += s;
+    }
+    int rc = ensure_segs(c, std::max(total, 1LL));
+    if (rc) return rc;
+    long long k = 0;
+    for (int i = 0; i < ntrials; i++)
+        for (long long s = 0; s < nsteps[i]; s++, k++) {
+            SegDesc& d = c->h_segs[k];
+            d.spec = spec[i];
+            d.numbins = numbins[i];
+            d.startr = rlo[i] + s * half;
+            d.trial = i;
+            d.step = (int)s;
+        }
+    CK(cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), c->stream));
+    if (total > 0)
+        CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
+                           c->stream));
+    for (long long g = 0; g < total; g += c->chunk) {
+        int n = (int)std::min<long long>(c->chunk, total - g);
+        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true);
+        if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    prof_collect(c);
+    unsigned long long nraw = *c->h_ncand;
+    c->last_raw = nraw;
+    long long keep = (long long)std::min<unsigned long long>(nraw, (unsigned long long)c->cand_cap);
+    std::vector<RawCand> raw(keep);
+    if (keep > 0)
+        CK(cudaMemcpy(raw.data(), c->d_cands, sizeof(RawCand) * keep, cudaMemcpyDeviceToHost));
+    c->results.clear();
+    c->results.reserve(keep);
+    for (const RawCand& r : raw) {
+        const SegDesc& d = c->h_segs[r.seg];
+        accel_candidate o;
+        o.trial = d.trial;
+        o.step = d.step;
+        o.r = (double)d.startr + 0.5 * r.ridx;
+        o.z = (double)(c->zlo0 + kDz * r.zidx);
+        o.numharm = r.numharm;
+        o.power = r.power;
+        o.sigma = (float)sigma_of_power(r.power, r.numharm, c->cfg.numindep);
+        c->results.push_back(o);
+    }
+    std::sort(c->results.begin(), c->results.end(), [](const accel_candidate& a, const accel_candidate& b) {
+        if (a.trial != b.trial) return a.trial < b.trial;
+        if (a.step != b.step) return a.step < b.step;
+        if (a.numharm != b.numharm) return a.numharm < b.numharm;
+        if (a.z != b.z) return a.z < b.z;
+        return a.r < b.r;
+    });
+    if (nraw > (unsigned long long)c->cand_cap)
+        return set_err(ACCEL_ERR_CAPACITY, "%llu candidates exceed the capacity of %lld", nraw,
+                       c->cand_cap);
+    return ACCEL_OK;
+}
+
+void free_ctx(accel_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (auto& kv : c->fftplans) cufftDestroy(kv.second);
+    for (auto& e : c->pending) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    for (auto e : c->evpool) cudaEventDestroy(e);
+    for (auto& kv : c->wplans) {
+        cudaFree(kv.second.d_start);
+        cudaFree(kv.second.d_len);
+        cudaFree(kv.second.d_med);
+    }
+    for (auto& t : c->trials) {
+        cudaFree(t.series);
+        cudaFree(t.spec);
+    }
+    cudaFree(c->bank_mem);
+    cudaFree(c->d_bh);
+    cudaFree(c->tw);
+    cudaFree(c->dbuf);
+    cudaFree(c->planes);
+    cudaFree(c->d_segs);
+    cudaFreeHost(c->h_segs);
+    cudaFree(c->d_cands);
+    cudaFree(c->d_ncand);
+    cudaFreeHost(c->h_ncand);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char* accel_version(void) { return "gpu_accelsearch_gb300 0.1 (sm_103a)"; }
+const char* accel_last_error(void) { return g_err.c_str(); }
+
+void accel_config_init(accel_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->zmax = 200;
+    cfg->numharm = 8;
+    cfg->fftlen = 8192;
+    cfg->uselen = 0;
+    cfg->whiten_initbuf = 6;
+    cfg->whiten_maxbuf = 200;
+    cfg->sigma = 6.0;
+    cfg->numindep = 1.0;
+    cfg->template_fp16 = 0;
+    cfg->chunk_segments = 0;
+    cfg->cand_capacity = 0;
+    cfg->device = 0;
+}
+
+int accel_create(const accel_config* cfg, accel_ctx** out) {
+    if (!cfg || !out) return set_err(ACCEL_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->zmax < 0 || (cfg->zmax & 1)) return set_err(ACCEL_ERR_INVALID, "zmax must be even and >= 0");
+    if (cfg->numharm < 1 || cfg->numharm > kMaxHarm || (cfg->numharm & (cfg->numharm - 1)))
+        return set_err(ACCEL_ERR_INVALID, "numharm must be 1, 2, 4, 8 or 16");
+    if (cfg->fftlen < 2 * kMinM || cfg->fftlen > 2 * kMaxM || (cfg->fftlen & (cfg->fftlen - 1)))
+        return set_err(ACCEL_ERR_UNSUPPORTED, "fftlen must be a power of two in [128, 16384]");
+    if (cfg->whiten_initbuf < 1 || cfg->whiten_maxbuf < 1)
+        return set_err(ACCEL_ERR_INVALID, "whitening block widths must be positive");
+    int U = cfg->uselen;
+    if (U <= 0) U = (cfg->fftlen - 2 - 2 * kNumBetween * z_halfwidth((double)cfg->zmax)) & ~1;
+    if (U < 2 || (U & 1) || U >= 65536)
+        return set_err(ACCEL_ERR_INVALID, "uselen %d must be even, positive and < 65536", U);
+    if (next_pow2((long long)U + 2 + 2 * kNumBetween * z_halfwidth((double)cfg->zmax)) != cfg->fftlen)
+        return set_err(ACCEL_ERR_INVALID, "uselen %d does not give segment length %d", U, cfg->fftlen);
+    accel_ctx* c = new accel_ctx();
+    c->cfg = *cfg;
+    c->device = cfg->device;
+    c->uselen = U;
+    int rc = ensure_device(c);
+    if (!rc) {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) rc = set_err(ACCEL_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+        c->own_stream = true;
+    }
+    if (!rc) {
+        cudaError_t e = cudaMalloc(&c->tw, sizeof(float2) * kTwN);
+        if (e != cudaSuccess) rc = set_err(ACCEL_ERR_NOMEM, "twiddles: %s", cudaGetErrorString(e));
+        else if (launch_twiddles(c->tw, c->stream) != 0) rc = set_err(ACCEL_ERR_CUDA, "twiddle launch");
+    }
+    if (!rc) rc = build_bank(c);
+    if (!rc) rc = build_plan(c);
+    if (!rc) rc = alloc_work(c);
+    if (rc) {
+        free_ctx(c);
+        return rc;
+    }
+    *out = c;
+    return ACCEL_OK;
+}
+
+int accel_destroy(accel_ctx* c) {
+    free_ctx(c);
+    return ACCEL_OK;
+}
+
+int accel_set_stream(accel_ctx* c, void* s) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+        c->own_stream = false;
+        c->stream = nullptr;
+    }
+    if (s) {
+        c->stream = (cudaStream_t)s;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return ACCEL_OK;
+}
+
+int accel_synchronize(accel_ctx* c) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return ACCEL_OK;
+}
+
+int accel_profile(accel_ctx* c, int enable) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    c->profiling = enable != 0;
+    return ACCEL_OK;
+}
+
+int accel_get_stats(accel_ctx* c, accel_stats* out) {
+    if (!c || !out) return set_err(ACCEL_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    prof_collect(c);
+    *out = c->stats;
+    return ACCEL_OK;
+}
+
+int accel_reset_stats(accel_ctx* c) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    prof_collect(c);
+    c->stats = accel_stats{};
+    return ACCEL_OK;
+}
+
+int accel_num_harmonics(const accel_ctx* c) { return c ? c->nh : 0; }
+int accel_num_stages(const accel_ctx* c) { return c ? c->nstages : 0; }
+int accel_uselen(const accel_ctx* c) { return c ? c->uselen : 0; }
+
+int accel_harmonic_info(const accel_ctx* c, int h, accel_harmonic* o) {
+    if (!c || !o || h < 0 || h >= c->nh) return set_err(ACCEL_ERR_INVALID, "bad harmonic index");
+    const BankHarmDev& b = c->bh[h];
+    o->harmnum = b.harmnum;
+    o->maxharm = b.maxharm;
+    o->zmax = b.zmax;
+    o->numzs = b.numzs;
+    o->fftlen = 2 * b.M;
+    o->halfwidth = b.hw0;
+    o->zlo = b.zlo;
+    o->plane_width = c->hp[h].wmax;
+    return ACCEL_OK;
+}
+
+int accel_get_power_cuts(const accel_ctx* c, float* cuts) {
+    if (!c || !cuts) return set_err(ACCEL_ERR_INVALID, "null argument");
+    for (int s = 0; s < c->nstages; s++) cuts[s] = c->cuts[s];
+    return ACCEL_OK;
+}
+
+int accel_set_power_cuts(accel_ctx* c, const float* cuts) {
+    if (!c || !cuts) return set_err(ACCEL_ERR_INVALID, "null argument");
+    for (int s = 0; s < c->nstages; s++) c->cuts[s] = cuts[s];
+    return ACCEL_OK;
+}
+
+long long accel_first_bin(long long nsamples, double dt) {
+    // AccelSearch.cu:101: long * float evaluated in single precision
+    return (long long)std::floor(1.0 * (double)((float)nsamples * (float)dt));
+}
+
+long long accel_step_count(const accel_ctx* c, long long nsamples, double dt) {
+    if (!c) return -1;
+    const long long half = (unsigned short)(c->uselen / 2);
+    long long rlo = accel_first_bin(nsamples, dt), numbins = nsamples / 2, s = 0;
+    for (long long r = rlo; r + half < numbins; r += half) s++;
+    return s;
+}
+
+int accel_step_harmonic(long long startr, int uselen, int harmnum, int maxharm, int hw0, long long* out) {
+    if (!out || harmnum < 1 || maxharm < 1 || uselen < 2) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    StepHarm g = step_harm(startr, uselen, harmnum, maxharm, hw0);
+    out[0] = g.rlo;
+    out[1] = g.ceilhi;
+    out[2] = g.numrs;
+    out[3] = g.lobin;
+    out[4] = g.numdata;
+    return ACCEL_OK;
+}
+
+int accel_harmonic_indices(long long startr, int uselen, int harmnum, int maxharm, int hw0, int zlo0,
+                           int zlo_h, int nr, int nz, int* rind, int* zind) {
+    if (harmnum < 1 || maxharm < 1 || nr < 0 || nz < 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    StepHarm g = step_harm(startr, uselen, harmnum, maxharm, hw0);
+    for (int i = 0; rind && i < nr; i++) rind[i] = sub_rind(startr, i, harmnum, maxharm, g.rlo);
+    for (int z = 0; zind && z < nz; z++) zind[z] = sub_zind(zlo0 + kDz * z, harmnum, maxharm, zlo_h);
+    return ACCEL_OK;
+}
+
+int accel_whiten(accel_ctx* c, accel_complex* spec, long long numbins) {
+    if (!c || !spec || numbins <= 0 || numbins > 0xffffffffLL) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (rc) return rc;
+    return do_whiten(c, reinterpret_cast<float2*>(spec), (unsigned)numbins);
+}
+
+int accel_rfft(accel_ctx* c, const float* series, long long n, accel_complex* spec) {
+    if (!c || !series || !spec || n < 2 || (n & 1)) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (rc) return rc;
+    return do_rfft(c, series, n, reinterpret_cast<float2*>(spec));
+}
+
+int accel_search(accel_ctx* c, int ntrials, const float* const* series, const long long* nsamples,
+                 const double* dt, int on_device, long long* ncand) {
+    if (!c || ntrials < 0 || (ntrials > 0 && (!series || !nsamples || !dt)))
+        return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (rc) return rc;
+    if ((int)c->trials.size() < ntrials) c->trials.resize(ntrials);
+    std::vector<float2*> specs(ntrials);
+    std::vector<long long> nb(ntrials), rlo(ntrials);
+    for (int i = 0; i < ntrials; i++) {
+        long long n = nsamples[i];
+        if (n < 4 || (n & 1) || n / 2 > 0x7fffffffLL)
+            return set_err(ACCEL_ERR_INVALID, "trial %d: sample count %lld must be even and >= 4", i, n);
+        TrialBuf& t = c->trials[i];
+        if (t.n < n) {
+            cudaFree(t.series);
+            cudaFree(t.spec);
+            t.series = nullptr;
+            t.spec = nullptr;
+            t.n = 0;
+            CK(cudaMalloc(&t.series, sizeof(float) * n));
+            CK(cudaMalloc(&t.spec, sizeof(float2) * (n / 2 + 1)));
+            t.n = n;
+        }
+        const float* src = series[i];
+        if (!on_device) {
+            CK(cudaMemcpyAsync(t.series, series[i], sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+            src = t.series;
+        }
+        rc = do_rfft(c, src, n, t.spec);
+        if (rc) return rc;
+        rc = do_whiten(c, t.spec, (unsigned)(n / 2));
+        if (rc) return rc;
+        specs[i] = t.spec;
+        nb[i] = n / 2;
+        rlo[i] = accel_first_bin(n, dt[i]);
+    }
+    rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data());
+    if (ncand) *ncand = (long long)c->last_raw;
+    return rc;
+}
+
+int accel_search_spectra(accel_ctx* c, int ntrials, const accel_complex* const* wspec,
+                         const long long* numbins, const long long* rlo, long long* ncand) {
+    if (!c || ntrials < 0 || (ntrials > 0 && (!wspec || !numbins || !rlo)))
+        return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (rc) return rc;
+    std::vector<float2*> specs(ntrials);
+    for (int i = 0; i < ntrials; i++) specs[i] = (float2*)wspec[i];
+    rc = run_search(c, ntrials, specs.data(), numbins, rlo);
+    if (ncand) *ncand = (long long)c->last_raw;
+    return rc;
+}
+
+int accel_candidates(accel_ctx* c, accel_candidate* out, long long cap, long long* n) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    long long m = std::min<long long>(cap, (long long)c->results.size());
+    if (out && m > 0) std::memcpy(out, c->results.data(), sizeof(accel_candidate) * m);
+    if (n) *n = (long long)c->results.size();
+    return ACCEL_OK;
+}
+
+int accel_layout(const accel_ctx* c, long long* dstride, long long* doff, long long* pstride,
+                 long long* poff, int* prow) {
+    if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    if (dstride) *dstride = c->dstride;
+    if (pstride) *pstride = c->pstride;
+    for (int h = 0; h < c->nh; h++) {
+        if (doff) doff[h] = c->hp[h].doff;
+        if (poff) poff[h] = c->hp[h].poff;
+        if (prow) prow[h] = c->hp[h].prow;
+    }
+    return ACCEL_OK;
+}
+
+static int stage_segs(accel_ctx* c, const float2* spec, long long numbins, const long long* startr, int nseg) {
+    int rc = ensure_segs(c, nseg);
+    if (rc) return rc;
+    for (int s = 0; s < nseg; s++) {
+        SegDesc& d = c->h_segs[s];
+        d.spec = spec;
+        d.numbins = numbins;
+        d.startr = startr[s];
+        d.trial = 0;
+        d.step = s;
+    }
+    CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * nseg, cudaMemcpyHostToDevice, c->stream));
+    return ACCEL_OK;
+}
+
+int accel_prepare_segments(accel_ctx* c, const accel_complex* wspec, long long numbins,
+                           const long long* startr, int nseg, accel_complex* dhalf) {
+    if (!c || !wspec || !startr || !dhalf || nseg <= 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (!rc) rc = stage_segs(c, (const float2*)wspec, numbins, startr, nseg);
+    if (!rc) rc = run_group(c, c->d_segs, nseg, 0, nullptr, (float2*)dhalf, nullptr, true, false, false);
+    if (!rc) CK(cudaStreamSynchronize(c->stream));
+    return rc;
+}
+
+int accel_power_planes(accel_ctx* c, const accel_complex* dhalf, int nseg, float* planes) {
+    if (!c || !dhalf || !planes || nseg <= 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (!rc) rc = run_group(c, c->d_segs, nseg, 0, nullptr, (const float2*)dhalf, planes, false, true, false);
+    if (!rc) CK(cudaStreamSynchronize(c->stream));
+    return rc;
+}
+
+int accel_sum_harmonics(accel_ctx* c, const float* planes, const long long* startr, int nseg,
+                        float* stage_out, long long* ncand) {
+    if (!c || !planes || !startr || nseg <= 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    int rc = ensure_device(c);
+    if (!rc) rc = stage_segs(c, nullptr, 0, startr, nseg);
+    if (!rc) CK(cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), c->stream));
+    if (!rc) rc = run_group(c, c->d_segs, nseg, 0, stage_out, nullptr, const_cast<float*>(planes), false, false, true);
+    if (!rc) {
+        CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (ncand) *ncand = (long long)*c->h_ncand;
+    }
+    return rc;
+}
+
+int accel_bank_spectra(const accel_ctx* c, int h, accel_complex* kstd, accel_complex* fold) {
+    if (!c || h < 0 || h >= c->nh) return set_err(ACCEL_ERR_INVALID, "bad harmonic index");
+    const BankHarmDev& b = c->bh[h];
+    size_t n = (size_t)b.numzs * 2 * b.M;
+    CK(cudaSetDevice(c->device));
+    if (kstd) CK(cudaMemcpy(kstd, b.kstd, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+    if (fold) CK(cudaMemcpy(fold, b.fold, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+    return ACCEL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// whiten.cu -- red-noise removal (deredden, bpd_noise.c:12-92) on the GPU.
+//
+// The reference walks the spectrum serially: block medians of growing
+// width (initialbuflen*ln(binnum), capped at maxbuflen), a linear slope
+// between neighbouring block levels, and amplitude *= rsqrt(level).  The
+// block boundaries are a serial recurrence and are planned on the host
+// (plan_whiten_blocks in api.cu); everything else is parallel:
+//   k_whiten_medians  one CTA per block: exact lower median of |A|^2
+//                     (radix select), level = median / ln 2 in double;
+//   k_whiten_scale    one CTA per write range: the range's level and slope
+//                     from its two neighbouring blocks, then the scaling
+//                     with the reference's float arithmetic.
+// Results are bit-identical to the reference's host routine.
+#include "accel_internal.h"
+
+namespace accel {
+
+constexpr double kLn2w = 0.693147180559945309417232121458;
+
+__global__ void __launch_bounds__(256) k_whiten_medians(const int* __restrict__ bstart,
+                                                        const int* __restrict__ blen,
+                                                        const float2* __restrict__ spec, double* med) {
+    extern __shared__ uint32_t keys[];
+    __shared__ int hist[256];
+    __shared__ int bc[2];
+    const int b = blockIdx.x;
+    const int s = bstart[b], n = blen[b];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = __float_as_uint(power_exact(spec[s + i]));
+    __syncthreads();
+    const uint32_t k = block_select_u32(keys, n, (n - 1) / 2, hist, bc);
+    if (threadIdx.x == 0) med[b] = (double)__uint_as_float(k) / kLn2w;
+}
+
+// Write range r (0 <= r <= nb): r = 0 is the first half-block with a flat
+// level; 1 <= r < nb interpolate from block r-1 towards block r; r = nb is
+// the tail, continuing the last slope (1.0 when there was no second block).
+__global__ void __launch_bounds__(256) k_whiten_scale(const int* __restrict__ bstart,
+                                                      const int* __restrict__ blen,
+                                                      const double* __restrict__ med, int nb,
+                                                      float2* spec, unsigned numbins) {
+    const int r = blockIdx.x;
+    long long lo, hi;
+    float mean_old, dslope;
+    if (r == 0) {
+        lo = 1;
+        hi = bstart[0] + blen[0] / 2;
+        mean_old = (float)med[0];
+        dslope = 0.f;
+        if (threadIdx.x == 0) spec[0] = make_float2(1.0f, 0.0f);
+    } else if (r < nb) {
+        lo = bstart[r - 1] + blen[r - 1] / 2;
+        hi = bstart[r] + blen[r] / 2;
+        mean_old = (float)med[r - 1];
+        dslope = (float)((med[r] - (double)mean_old) / (0.5 * (blen[r - 1] + blen[r])));
+    } else {
+        lo = bstart[nb - 1] + blen[nb - 1] / 2;
+        hi = numbins;
+        mean_old = (float)med[nb - 1];
+        if (nb >= 2) {
+            const float mo = (float)med[nb - 2];
+            dslope = (float)((med[nb - 1] - (double)mo) / (0.5 * (blen[nb - 2] + blen[nb - 1])));
+        } else {
+            dslope = 1.0f;
+        }
+    }
+    const float flat = rsqrt_magic(mean_old);
+    for (long long ind = lo + threadIdx.x; ind < hi; ind += blockDim.x) {
+        float norm;
+        if (r == 0) norm = flat;
+        else norm = rsqrt_magic(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))));
+        float2 v = spec[ind];
+        v.x = __fmul_rn(v.x, norm);
+        v.y = __fmul_rn(v.y, norm);
+        spec[ind] = v;
+    }
+}
+
+int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
+                  unsigned numbins, int maxlen, cudaStream_t st) {
+    size_t smem = sizeof(uint32_t) * (size_t)maxlen;
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_whiten_medians, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+    }
+    k_whiten_medians<<<nblocks, 256, smem, st>>>(d_bstart, d_blen, spec, d_med);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    k_whiten_scale<<<nblocks + 1, 256, 0, st>>>(d_bstart, d_blen, d_med, nblocks, spec, numbins);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace accel

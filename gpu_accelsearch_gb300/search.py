@@ -1,0 +1,228 @@
+"""Python front end of the search: a thin, typed layer over the C ABI.
+
+`AccelSearch` mirrors the reference pipeline (keithasr/gpu_accelsearch):
+
+=============================  ==============================================
+reference                      here
+=============================  ==============================================
+createSubharmonicInfo          AccelSearch(zmax, numharm, fftlen) (bank built
+                               on the GPU at construction), .harmonics
+realToComplexFFT               .rfft(series_dev, spec_dev)
+deredden                       .whiten(spec_dev)
+generate_harmonic_ffdot_data   .prepare_segments(wspec_dev, startr, out_dev)
+ + perform_fft_harmonics
+perform_convolution            .power_planes(dhalf_dev, nseg, planes_dev)
+ + perform_inversefft
+ + generate_fundamental_powers
+perform_harmonic_summing       .sum_harmonics(planes_dev, startr, stage_dev)
+ + search_ffdot_powers
+main() step loop               .search(series, dt) / .search_spectra(...)
+=============================  ==============================================
+
+Device buffers are passed as integer device addresses (for example
+``torch.Tensor.data_ptr()``); host inputs as numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native as N
+
+
+@dataclass
+class HarmonicInfo:
+    harmnum: int
+    maxharm: int
+    zmax: int
+    numzs: int
+    fftlen: int
+    halfwidth: int
+    zlo: int
+    plane_width: int
+
+
+CAND_DTYPE = np.dtype([("trial", "i4"), ("step", "i4"), ("r", "f8"), ("z", "f8"),
+                       ("numharm", "i4"), ("power", "f4"), ("sigma", "f4")])
+
+
+def first_bin(nsamples: int, dt: float) -> int:
+    return N.lib().accel_first_bin(nsamples, dt)
+
+
+class AccelSearch:
+    def __init__(self, zmax=200, numharm=8, fftlen=8192, uselen=0, sigma=6.0, numindep=1.0,
+                 whiten_initbuf=6, whiten_maxbuf=200, template_fp16=False, chunk_segments=0,
+                 cand_capacity=0, device=0):
+        L = N.lib()
+        cfg = N.Config()
+        L.accel_config_init(C.byref(cfg))
+        cfg.zmax, cfg.numharm, cfg.fftlen, cfg.uselen = zmax, numharm, fftlen, uselen
+        cfg.sigma, cfg.numindep = sigma, numindep
+        cfg.whiten_initbuf, cfg.whiten_maxbuf = whiten_initbuf, whiten_maxbuf
+        cfg.template_fp16 = int(bool(template_fp16))
+        cfg.chunk_segments, cfg.cand_capacity, cfg.device = chunk_segments, cand_capacity, device
+        self.config = cfg
+        h = C.c_void_p()
+        N.check(L.accel_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.nh = L.accel_num_harmonics(h)
+        self.nstages = L.accel_num_stages(h)
+        self.uselen = L.accel_uselen(h)
+        self.harmonics = []
+        for i in range(self.nh):
+            hi = N.Harmonic()
+            N.check(L.accel_harmonic_info(h, i, C.byref(hi)))
+            self.harmonics.append(HarmonicInfo(*[getattr(hi, f) for f, _ in hi._fields_]))
+        ds, ps = C.c_longlong(), C.c_longlong()
+        doff = (C.c_longlong * self.nh)()
+        poff = (C.c_longlong * self.nh)()
+        prow = (C.c_int * self.nh)()
+        N.check(L.accel_layout(h, C.byref(ds), doff, C.byref(ps), poff, prow))
+        self.dhalf_stride, self.plane_stride = ds.value, ps.value
+        self.dhalf_off, self.plane_off = list(doff), list(poff)
+        self.plane_row = list(prow)
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().accel_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------- queries
+    def power_cuts(self):
+        a = (C.c_float * self.nstages)()
+        N.check(N.lib().accel_get_power_cuts(self._h, a))
+        return np.array(a, np.float32)
+
+    def set_power_cuts(self, cuts):
+        a = (C.c_float * self.nstages)(*[float(x) for x in cuts])
+        N.check(N.lib().accel_set_power_cuts(self._h, a))
+
+    def step_count(self, nsamples: int, dt: float) -> int:
+        return N.lib().accel_step_count(self._h, nsamples, dt)
+
+    def bank_spectra(self, h: int):
+        hi = self.harmonics[h]
+        k = np.zeros((hi.numzs, hi.fftlen), np.complex64)
+        f = np.zeros((hi.numzs, hi.fftlen), np.complex64)
+        N.check(N.lib().accel_bank_spectra(self._h, h, k.ctypes.data, f.ctypes.data))
+        return k, f
+
+    def profile(self, enable: bool = True):
+        N.check(N.lib().accel_profile(self._h, int(enable)))
+
+    def stats(self) -> dict:
+        st = N.Stats()
+        N.check(N.lib().accel_get_stats(self._h, C.byref(st)))
+        return {"launches": st.launches, "segments": st.segments, "cells": st.cells,
+                "kinds": {k: {"launches": st.kind_launches[i], "ms": st.kind_ms[i]}
+                          for i, k in enumerate(N.KINDS)}}
+
+    def reset_stats(self):
+        N.check(N.lib().accel_reset_stats(self._h))
+
+    # -------------------------------------------------------------- stages
+    def synchronize(self):
+        N.check(N.lib().accel_synchronize(self._h))
+
+    def rfft(self, series_dev: int, n: int, spec_dev: int):
+        N.check(N.lib().accel_rfft(self._h, series_dev, n, spec_dev))
+
+    def whiten(self, spec_dev: int, numbins: int):
+        N.check(N.lib().accel_whiten(self._h, spec_dev, numbins))
+
+    def prepare_segments(self, wspec_dev: int, numbins: int, startr, out_dev: int):
+        s = np.ascontiguousarray(startr, dtype=np.int64)
+        N.check(N.lib().accel_prepare_segments(self._h, wspec_dev, numbins,
+                                               s.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                               s.size, out_dev))
+
+    def power_planes(self, dhalf_dev: int, nseg: int, planes_dev: int):
+        N.check(N.lib().accel_power_planes(self._h, dhalf_dev, nseg, planes_dev))
+
+    def sum_harmonics(self, planes_dev: int, startr, stage_dev: int = 0) -> int:
+        s = np.ascontiguousarray(startr, dtype=np.int64)
+        n = C.c_longlong()
+        N.check(N.lib().accel_sum_harmonics(self._h, planes_dev,
+                                            s.ctypes.data_as(C.POINTER(C.c_longlong)), s.size,
+                                            stage_dev or None, C.byref(n)))
+        return n.value
+
+    # -------------------------------------------------------------- search
+    def search(self, series, dt, on_device=False, nsamples=None):
+        """series: list of float32 numpy arrays (host) or device addresses."""
+        n = len(series)
+        ptrs = (C.c_void_p * n)()
+        ns = (C.c_longlong * n)()
+        dts = (C.c_double * n)()
+        dtl = dt if isinstance(dt, (list, tuple, np.ndarray)) else [dt] * n
+        keep = []
+        for i, s in enumerate(series):
+            if on_device:
+                ptrs[i] = int(s)
+                ns[i] = int(nsamples[i])
+            else:
+                a = np.ascontiguousarray(s, dtype=np.float32)
+                keep.append(a)
+                ptrs[i] = a.ctypes.data
+                ns[i] = a.size
+            dts[i] = float(dtl[i])
+        nc = C.c_longlong()
+        N.check(N.lib().accel_search(self._h, n, ptrs, ns, dts, int(bool(on_device)), C.byref(nc)))
+        return nc.value
+
+    def search_ptrs(self, ptrs, nsamples, dt, on_device: bool) -> int:
+        """Search series given as raw addresses (device, or pinned host)."""
+        n = len(ptrs)
+        pa = (C.c_void_p * n)(*[int(p) for p in ptrs])
+        ns = (C.c_longlong * n)(*[int(x) for x in nsamples])
+        dtl = dt if isinstance(dt, (list, tuple, np.ndarray)) else [dt] * n
+        dts = (C.c_double * n)(*[float(x) for x in dtl])
+        nc = C.c_longlong()
+        N.check(N.lib().accel_search(self._h, n, pa, ns, dts, int(bool(on_device)), C.byref(nc)))
+        return nc.value
+
+    def search_spectra(self, wspec_devs, numbins, rlo):
+        n = len(wspec_devs)
+        ptrs = (C.c_void_p * n)(*[int(p) for p in wspec_devs])
+        nb = (C.c_longlong * n)(*[int(x) for x in numbins])
+        rl = (C.c_longlong * n)(*[int(x) for x in rlo])
+        nc = C.c_longlong()
+        N.check(N.lib().accel_search_spectra(self._h, n, ptrs, nb, rl, C.byref(nc)))
+        return nc.value
+
+    def candidates(self) -> np.ndarray:
+        L = N.lib()
+        n = C.c_longlong()
+        N.check(L.accel_candidates(self._h, None, 0, C.byref(n)))
+        buf = (N.Candidate * max(n.value, 1))()
+        N.check(L.accel_candidates(self._h, buf, n.value, C.byref(n)))
+        out = np.zeros(n.value, CAND_DTYPE)
+        raw = np.frombuffer(buf, dtype=np.uint8, count=n.value * C.sizeof(N.Candidate))
+        if n.value:
+            view = np.ndarray(n.value, dtype=np.dtype({
+                "names": ["trial", "step", "r", "z", "numharm", "power", "sigma"],
+                "formats": ["i4", "i4", "f8", "f8", "i4", "f4", "f4"],
+                "offsets": [N.Candidate.trial.offset, N.Candidate.step.offset,
+                            N.Candidate.r.offset, N.Candidate.z.offset,
+                            N.Candidate.numharm.offset, N.Candidate.power.offset,
+                            N.Candidate.sigma.offset],
+                "itemsize": C.sizeof(N.Candidate)}), buffer=raw)
+            for f in CAND_DTYPE.names:
+                out[f] = view[f]
+        return out

@@ -1,0 +1,169 @@
+/*
+ * accelsearch.h -- C ABI of libaccelsearch.so, a GB300 (sm_103a)
+ * Fourier-domain acceleration search.
+ *
+ * Two layers:
+ *
+ *  1. The context API (accel_*).  Every call returns an int status
+ *     (ACCEL_OK or a negative ACCEL_ERR_*), never exits, and leaves a
+ *     message for accel_last_error() (per host thread).  All device work of a
+ *     context is issued on its stream; one context per host thread.
+ *
+ *  2. Drop-in entry points with the reference's names and argument meaning
+ *     (keithasr/gpu_accelsearch, headers/bpd_*.h / *.cuh), for callers of
+ *     that pipeline API.  They run on a process-wide default context, as the
+ *     reference keeps its plans and streams in process globals
+ *     (bpd_search.cu:10-13).  accel_complex is layout-compatible with
+ *     cufftComplex.  Each declaration cites the reference interface it
+ *     replaces.
+ *
+ * All pointers named *_dev are device pointers; all others are host memory.
+ */
+#ifndef ACCELSEARCH_H_
+#define ACCELSEARCH_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACCEL_OK               0
+#define ACCEL_ERR_INVALID     -1   /* bad argument or configuration        */
+#define ACCEL_ERR_CUDA        -2   /* a CUDA runtime or launch error        */
+#define ACCEL_ERR_NOMEM       -3   /* device or host allocation failed      */
+#define ACCEL_ERR_CAPACITY    -4   /* candidate buffer overflowed           */
+#define ACCEL_ERR_UNSUPPORTED -5   /* outside the built kernel shapes       */
+#define ACCEL_ERR_BUDGET      -6   /* request exceeds the HBM budget        */
+
+typedef struct { float x, y; } accel_complex;   /* == cufftComplex */
+
+typedef struct accel_config {
+    int zmax;               /* largest |f-dot| (bins), even; reference zhi       */
+    int numharm;            /* harmonics summed: 1, 2, 4, 8 or 16                */
+    int fftlen;             /* fundamental segment length L (power of two)       */
+    int uselen;             /* 0: derived, L - 2 - 4*halfwidth(zmax), even       */
+    int whiten_initbuf;     /* first whitening block (reference: 6)              */
+    int whiten_maxbuf;      /* largest whitening block (reference: 200)          */
+    double sigma;           /* candidate threshold in Gaussian sigma (6)         */
+    double numindep;        /* trial-count divisor of the tail probability (1)   */
+    int template_fp16;      /* 1: FP16 folded templates, scaled per template     */
+    int chunk_segments;     /* segments per launch group (0: automatic)          */
+    long long cand_capacity;/* raw candidates kept per search (0: automatic)     */
+    int device;             /* CUDA device ordinal                               */
+    int reserved[7];
+} accel_config;
+
+typedef struct accel_harmonic {
+    int harmnum, maxharm;   /* harmonic fraction harmnum/maxharm                 */
+    int zmax, numzs;        /* templates z = -zmax .. zmax step 2                */
+    int fftlen;             /* segment length L_h                                */
+    int halfwidth;          /* halfwidth of the widest template (binOffset)      */
+    int zlo;                /* lowest f-dot of the harmonic's plane              */
+    int plane_width;        /* powers per f-dot row kept on the device           */
+} accel_harmonic;
+
+typedef struct accel_candidate {
+    int trial;              /* index of the time series in the search call       */
+    int step;               /* overlap-save step within the trial                */
+    double r;               /* Fourier frequency of the fundamental (bins)       */
+    double z;               /* f-dot of the fundamental (bins)                   */
+    int numharm;            /* harmonics summed                                  */
+    float power;            /* summed normalised power                           */
+    float sigma;            /* equivalent Gaussian significance                  */
+} accel_candidate;
+
+/* Kernel accounting of a context (accel_get_stats).  Kinds: 0 segment
+ * preparation, 1 power planes, 2 harmonic sum, 3 whitening, 4 R2C FFT
+ * (cuFFT; not counted in `launches`). */
+#define ACCEL_KINDS 5
+typedef struct accel_stats {
+    long long launches;                 /* kernels of this library launched   */
+    long long kind_launches[ACCEL_KINDS];
+    double kind_ms[ACCEL_KINDS];        /* CUDA-event time when profiling      */
+    long long segments;                 /* overlap-save steps searched         */
+    long long cells;                    /* fundamental f-fdot cells searched   */
+} accel_stats;
+
+typedef struct accel_ctx accel_ctx;
+
+/* ---------------------------------------------------------------- context */
+const char *accel_version(void);
+const char *accel_last_error(void);
+void accel_config_init(accel_config *cfg);
+int  accel_create(const accel_config *cfg, accel_ctx **out);
+int  accel_destroy(accel_ctx *ctx);
+/* Run all further work of ctx on this cudaStream_t (NULL: the context's own). */
+int  accel_set_stream(accel_ctx *ctx, void *cuda_stream);
+int  accel_synchronize(accel_ctx *ctx);
+/* Time every kernel with CUDA events on the context's stream (1) or not (0). */
+int  accel_profile(accel_ctx *ctx, int enable);
+int  accel_get_stats(accel_ctx *ctx, accel_stats *out);
+int  accel_reset_stats(accel_ctx *ctx);
+
+int  accel_num_harmonics(const accel_ctx *ctx);
+int  accel_num_stages(const accel_ctx *ctx);
+int  accel_uselen(const accel_ctx *ctx);
+int  accel_harmonic_info(const accel_ctx *ctx, int h, accel_harmonic *out);
+/* Power cuts per stage (1, 2, 4, ... harmonics), float[num_stages]. */
+int  accel_get_power_cuts(const accel_ctx *ctx, float *cuts);
+int  accel_set_power_cuts(accel_ctx *ctx, const float *cuts);
+/* Search geometry of a series of n samples at dt seconds (host only):
+ * first bin rlo = floor(n*dt) (AccelSearch.cu:101) and the number of
+ * overlap-save steps (AccelSearch.cu:209). */
+long long accel_first_bin(long long nsamples, double dt);
+long long accel_step_count(const accel_ctx *ctx, long long nsamples, double dt);
+/* Geometry of one harmonic (harmnum/maxharm, widest halfwidth hw0) for the
+ * step starting at startr (generate_harmonics_ffdot, bpd_search.cu:72-127,
+ * and the segment bounds of :138-144), host only.  out[0..4] = rlo,
+ * ceil(rhi), numrs, lobin, numdata. */
+int  accel_step_harmonic(long long startr, int uselen, int harmnum, int maxharm, int hw0,
+                         long long *out);
+/* addPowers index arithmetic (bpd_gpu_kernels.cu:139-153), host only: the
+ * sub-harmonic column rind[i] of fundamental column i < nr and the
+ * sub-harmonic row zind[z] of fundamental row z < nz (fundamental zlo0,
+ * sub-harmonic zlo_h). */
+int  accel_harmonic_indices(long long startr, int uselen, int harmnum, int maxharm, int hw0,
+                            int zlo0, int zlo_h, int nr, int nz, int *rind, int *zind);
+
+/* ------------------------------------------------------------ whole search */
+/* Search ntrials time series: R2C FFT, whitening, every overlap-save step,
+ * harmonic summing and thresholding.  series[i] holds nsamples[i] float32
+ * samples (host memory, or device memory when series_on_device).  Returns
+ * the number of candidates in *ncand; fetch them with accel_candidates. */
+int  accel_search(accel_ctx *ctx, int ntrials, const float *const *series,
+                  const long long *nsamples, const double *dt, int series_on_device,
+                  long long *ncand);
+/* The same from whitened spectra already on the device (bins [0, numbins)). */
+int  accel_search_spectra(accel_ctx *ctx, int ntrials, const accel_complex *const *wspec_dev,
+                          const long long *numbins, const long long *rlo, long long *ncand);
+/* Candidates of the last search, sorted by (trial, step, numharm, z, r). */
+int  accel_candidates(accel_ctx *ctx, accel_candidate *out, long long cap, long long *n);
+
+/* ------------------------------------------------------------ stage calls */
+/* Whitening in place (deredden, bpd_noise.c:12-92). */
+int  accel_whiten(accel_ctx *ctx, accel_complex *spec_dev, long long numbins);
+/* Real-to-complex FFT of a device series into spec_dev (n/2+1 bins). */
+int  accel_rfft(accel_ctx *ctx, const float *series_dev, long long n, accel_complex *spec_dev);
+/* Segment spectra of nseg steps (first bins startr[]): per step and
+ * harmonic the M_h = L_h/2 point spectrum of the normalised segment, packed
+ * at dhalf_dev + s*segment_stride + offset_h (see accel_layout). */
+int  accel_prepare_segments(accel_ctx *ctx, const accel_complex *wspec_dev, long long numbins,
+                            const long long *startr, int nseg, accel_complex *dhalf_dev);
+/* Power planes of nseg steps from prepared segment spectra: per step and
+ * harmonic numzs_h rows of plane_width_h powers (row stride plane_stride_h). */
+int  accel_power_planes(accel_ctx *ctx, const accel_complex *dhalf_dev, int nseg, float *planes_dev);
+/* Harmonic sums of nseg steps from power planes; optional stage planes
+ * [nseg][nstages][numzs0][uselen]; candidates appended to the context. */
+int  accel_sum_harmonics(accel_ctx *ctx, const float *planes_dev, const long long *startr,
+                         int nseg, float *stage_dev, long long *ncand);
+/* Layout of the per-step buffers used above (elements, not bytes):
+ * dhalf: segment_stride, offsets[h];  planes: plane_stride, offsets[h],
+ * row strides[h]. */
+int  accel_layout(const accel_ctx *ctx, long long *dhalf_stride, long long *dhalf_off,
+                  long long *plane_stride, long long *plane_off, int *row_stride);
+/* Copy of the template bank: kstd [numzs][L_h] and fold [numzs][L_h]. */
+int  accel_bank_spectra(const accel_ctx *ctx, int h, accel_complex *kstd, accel_complex *fold);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACCELSEARCH_H_ */

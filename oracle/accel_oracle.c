@@ -583,6 +583,9 @@ long orc_run_steps(orc_ctx *c, const float *wspec, long numbins, long rlo, long 
                 int hrlo, hzlo, hnumrs;
                 double hrhi;
                 orc_step_ffdot(o[0], o[1], c->zmax, U, startr, lastr, &hrlo, &hrhi, &hzlo, &hnumrs);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
                 for (int z = 0; z < numzs0; z++) {
                     int zz = zlo0 + z * O_DZ;
                     int subz = (int)(zz * f);

@@ -1,0 +1,218 @@
+"""GPU path against the FP64 CPU oracle, through the C ABI.
+
+Tolerances (stated per check):
+  * template spectra: max |K - K64| / max |K64| < 2e-6 (FP32 storage of an
+    FP64 transform);
+  * whitening: bit-identical to the reference's routine (oracle restates it
+    operation for operation);
+  * segment spectra: max |D - D64| / max |D64| < 2e-5 (FP32 FFT);
+  * power planes and stage sums: max |P - P64| / max(P64, 1) < 1e-4, the
+    precision target of the search (noise powers have mean 1);
+  * candidates: identical sets outside a guard band of +-1e-4 relative
+    around each stage's power cut.
+"""
+import numpy as np
+import pytest
+
+from gpu_accelsearch_gb300.synth import synth_red_spectrum, synth_series
+from oracle import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL_P = 1e-4
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.float32).copy()).cuda()
+
+
+def host_c64(t):
+    return t.cpu().numpy().view(np.complex64)
+
+
+@pytest.fixture(scope="module")
+def S():
+    from gpu_accelsearch_gb300.search import AccelSearch
+    s = AccelSearch(zmax=50, numharm=4, fftlen=2048)
+    yield s
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def trial():
+    n, dt = 1 << 18, 64e-6
+    x = synth_series(n, seed=1018, signals=[(0.05, 20000.25, 40.0)])
+    spec = np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2]
+    w = O.deredden(spec)
+    return {"n": n, "dt": dt, "x": x, "w": w, "rlo": 16}
+
+
+@pytest.fixture(scope="module")
+def orc():
+    o = O.Oracle(50, 4, 1914)
+    yield o
+    o.close()
+
+
+def test_bank_spectra(S):
+    for h, hi in enumerate(S.harmonics):
+        k, f = S.bank_spectra(h)
+        L, M = hi.fftlen, hi.fftlen // 2
+        k64 = np.stack([O.fft64(O.wrapped_template(L, -hi.zmax + 2 * j)) for j in range(hi.numzs)])
+        err = np.abs(k - k64).max() / np.abs(k64).max()
+        assert err < 2e-6, (h, err)
+        ck = np.conj(k64)
+        a64 = ck[:, :M] + ck[:, M:]
+        b64 = (ck[:, :M] - ck[:, M:]) * np.exp(2j * np.pi * np.arange(M) / L)
+        ferr = np.abs(f - np.concatenate([a64, b64], axis=1)).max() / np.abs(a64).max()
+        assert ferr < 4e-6, (h, ferr)
+
+
+@pytest.mark.parametrize("numbins,init,maxb", [(1 << 17, 6, 200), (1 << 15, 6, 200),
+                                               (12345, 6, 200), (1 << 17, 1000, 1000)])
+def test_whitening_bit_exact(numbins, init, maxb):
+    from gpu_accelsearch_gb300.search import AccelSearch
+    spec = synth_red_spectrum(numbins + 1, seed=numbins)
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048, whiten_initbuf=init,
+                     whiten_maxbuf=maxb) as s:
+        d = dev(spec)
+        s.whiten(d.data_ptr(), numbins)
+        s.synchronize()
+        got = host_c64(d)
+    want = spec.copy()
+    want[:numbins] = O.deredden(spec[:numbins], init, maxb)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_segment_spectra(S, trial):
+    w = trial["w"]
+    startr = [16, 16 + 957, 16 + 957 * 70, 16 + 957 * 135]
+    out = torch.zeros(len(startr) * S.dhalf_stride * 2, dtype=torch.float32, device="cuda")
+    d = dev(w)
+    S.prepare_segments(d.data_ptr(), w.size, startr, out.data_ptr())
+    got = host_c64(out).reshape(len(startr), S.dhalf_stride)
+    U = S.uselen
+    for si, s0 in enumerate(startr):
+        for h, hi in enumerate(S.harmonics):
+            L, M = hi.fftlen, hi.fftlen // 2
+            rlo, rhi, _, _ = O.step_ffdot(hi.harmnum, hi.maxharm, 50, U, float(s0),
+                                          s0 + U // 2 - 0.5)
+            seg = O.segment_data(w, rlo, rhi, hi.halfwidth, L)
+            d64 = O.fft64(seg)[:M]
+            g = got[si, S.dhalf_off[h]: S.dhalf_off[h] + M]
+            err = np.abs(g - d64).max() / np.abs(d64).max()
+            assert err < 2e-5, (si, h, err)
+
+
+def _planes(S, w, startr):
+    d = dev(w)
+    nseg = len(startr)
+    dh = torch.zeros(nseg * S.dhalf_stride * 2, dtype=torch.float32, device="cuda")
+    pl = torch.zeros(nseg * S.plane_stride, dtype=torch.float32, device="cuda")
+    S.prepare_segments(d.data_ptr(), w.size, startr, dh.data_ptr())
+    S.power_planes(dh.data_ptr(), nseg, pl.data_ptr())
+    return d, dh, pl
+
+
+def test_power_planes(S, trial, orc):
+    w = trial["w"]
+    startr = [16 + 957 * 20, 16 + 957 * 21]   # step 20 holds the injected signal
+    _, _, pl = _planes(S, w, startr)
+    P = pl.cpu().numpy().reshape(len(startr), S.plane_stride)
+    worst = 0.0
+    for si, s0 in enumerate(startr):
+        for h, hi in enumerate(S.harmonics):
+            p64 = orc.harmonic_plane(w, float(s0), h)
+            nz, nr = p64.shape
+            g = P[si, S.plane_off[h]: S.plane_off[h] + nz * S.plane_row[h]].reshape(
+                nz, S.plane_row[h])[:, :nr]
+            err = (np.abs(g - p64) / np.maximum(p64, 1.0)).max()
+            worst = max(worst, err)
+            assert err < TOL_P, (si, h, err)
+    print("max relative power error", worst)
+
+
+def test_stage_sums(S, trial, orc):
+    w = trial["w"]
+    steps = [0, 20, 135]
+    startr = [16 + 957 * k for k in steps]
+    _, _, pl = _planes(S, w, startr)
+    ns, nz, U = S.nstages, S.harmonics[0].numzs, S.uselen
+    st = torch.zeros(len(steps) * ns * nz * U, dtype=torch.float32, device="cuda")
+    S.sum_harmonics(pl.data_ptr(), startr, st.data_ptr())
+    got = st.cpu().numpy().reshape(len(steps), ns, nz, U)
+    for si, k in enumerate(steps):
+        _, planes, _ = orc.run_steps(w, 16, k, 1, want_planes=True)
+        err = (np.abs(got[si] - planes[0]) / np.maximum(planes[0], 1.0)).max()
+        assert err < TOL_P, (k, err)
+
+
+def _keyset(a, rlo, half, zlo0):
+    if "ridx" in a.dtype.names:
+        return {(int(c["step"]), int(c["ridx"]), int(c["zidx"]), int(c["numharm"])) for c in a}
+    return {(int(c["step"]), int(round(2 * (c["r"] - (rlo + c["step"] * half)))),
+             int(round((c["z"] - zlo0) / 2)), int(c["numharm"])) for c in a}
+
+
+def test_candidates_match_oracle(S, trial, orc):
+    w, rlo = trial["w"], trial["rlo"]
+    d = dev(w)
+    n = S.search_spectra([d.data_ptr()], [w.size], [rlo])
+    gpu = S.candidates()
+    assert n == len(gpu)
+    nsteps = S.step_count(trial["n"], trial["dt"])
+    cuts = S.power_cuts().astype(np.float64)
+    o_lo, _, _ = orc.run_steps(w, rlo, 0, nsteps, powcut=cuts * (1 - TOL_P))
+    o_hi, _, _ = orc.run_steps(w, rlo, 0, nsteps, powcut=cuts * (1 + TOL_P))
+    g = _keyset(gpu, rlo, S.uselen // 2, -50)
+    assert _keyset(o_hi, 0, 0, 0) <= g <= _keyset(o_lo, 0, 0, 0)
+    assert len(g) > 0
+    # the injected signal is the strongest candidate, at r0 + z/2 and z
+    best = gpu[np.argmax(gpu["power"])]
+    assert abs(best["r"] - (20000.25 + 20.0)) <= 1.0 and abs(best["z"] - 40) <= 4
+
+
+def test_full_pipeline_from_time_series(S, trial):
+    # cuFFT R2C + GPU whitening + search, from a host series through the C ABI
+    n = S.search([trial["x"]], trial["dt"])
+    gpu = S.candidates()
+    assert n == len(gpu) > 0
+    best = gpu[np.argmax(gpu["power"])]
+    assert abs(best["r"] - 20020.25) <= 1.0 and abs(best["z"] - 40) <= 4
+    # and the device spectrum path gives the same candidates as the host one
+    xd = torch.from_numpy(trial["x"]).cuda()
+    n2 = S.search([xd.data_ptr()], trial["dt"], on_device=True, nsamples=[trial["n"]])
+    assert n2 == n
+    assert np.array_equal(S.candidates(), gpu)
+
+
+def test_whitened_pipeline_matches_host_whitening(S, trial):
+    # GPU rfft+whiten vs numpy rfft + oracle whitening: same candidates up to
+    # the FFT rounding of the input spectrum (strongest cell identical).
+    x = trial["x"]
+    xd = torch.from_numpy(x).cuda()
+    spec = torch.zeros((trial["n"] // 2 + 1) * 2, dtype=torch.float32, device="cuda")
+    S.rfft(xd.data_ptr(), trial["n"], spec.data_ptr())
+    S.synchronize()
+    got = host_c64(spec)[: trial["n"] // 2]
+    ref = np.fft.rfft(x.astype(np.float64))[: trial["n"] // 2]
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 1e-5, err
+
+
+def test_batched_equals_single(S, trial):
+    # segments of several trials in one launch group give the per-trial result
+    x1 = trial["x"]
+    x2 = synth_series(1 << 17, seed=77, signals=[(0.08, 9000.5, -30.0)])
+    S.search([x1], trial["dt"])
+    c1 = S.candidates()
+    S.search([x2], trial["dt"])
+    c2 = S.candidates()
+    S.search([x1, x2], trial["dt"])
+    cb = S.candidates()
+    c2b = c2.copy()
+    c2b["trial"] = 1
+    both = np.concatenate([c1, c2b])
+    assert np.array_equal(np.sort(cb, order=["trial", "step", "numharm", "z", "r"]),
+                          np.sort(both, order=["trial", "step", "numharm", "z", "r"]))

@@ -1,0 +1,116 @@
+"""C-ABI checks that need no GPU: the library loads, exports every function
+declared in include/accelsearch.h, validates configurations before touching
+the device, and computes the host-side search geometry like the reference."""
+import ctypes as C
+import os
+import math
+import re
+
+import pytest
+
+import __graft_entry__
+from gpu_accelsearch_gb300 import native as N
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    __graft_entry__.build_library()
+    return N.lib()
+
+
+def declared_functions():
+    names = []
+    for hdr in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not hdr.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", hdr)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", text, flags=re.M):
+            if m.group(1) not in ("if", "defined"):
+                names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_exports_every_declared_function(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding covers the header
+    assert set(N.exported_symbols()) <= set(names)
+
+
+def test_config_defaults(lib):
+    cfg = N.Config()
+    lib.accel_config_init(C.byref(cfg))
+    assert (cfg.zmax, cfg.numharm, cfg.fftlen, cfg.whiten_initbuf, cfg.whiten_maxbuf) == \
+        (200, 8, 8192, 6, 200)
+    assert cfg.sigma == 6.0
+
+
+@pytest.mark.parametrize("field,value", [("zmax", 3), ("numharm", 3), ("fftlen", 3000),
+                                         ("fftlen", 1 << 16), ("uselen", 7735),
+                                         ("uselen", 9000), ("whiten_maxbuf", 0)])
+def test_invalid_config_rejected_before_device(lib, field, value):
+    cfg = N.Config()
+    lib.accel_config_init(C.byref(cfg))
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    rc = lib.accel_create(C.byref(cfg), C.byref(h))
+    assert rc in (-1, -5), (rc, lib.accel_last_error())
+    assert not h.value
+
+
+def test_first_bin_matches_reference(lib):
+    # AccelSearch.cu:101 evaluates n * dt in single precision
+    for n, dt, want in [(1 << 18, 64e-6, 16), (1 << 22, 64e-6, 268), (3 << 20, 64e-6, 201),
+                        (1 << 20, 72e-6, 75)]:
+        assert lib.accel_first_bin(n, dt) == want
+
+
+def test_step_geometry_matches_oracle(lib):
+    # the integer geometry the kernels use vs the reference's double arithmetic
+    out = (C.c_longlong * 5)()
+    for zmax, numharm, U in [(50, 4, 1914), (200, 8, 7734), (200, 8, 3638), (200, 8, 15926)]:
+        geom = O.bank_geometry(zmax, numharm, U)
+        for startr in (16, 957, 20000, 268, 268 + 3867 * 541, 123457, 999999):
+            lastr = startr + U // 2 - 0.5
+            for g in geom:
+                p, q, hw0 = int(g[0]), int(g[1]), int(g[5])
+                rlo, rhi, zlo, numrs = O.step_ffdot(p, q, zmax, U, float(startr), lastr)
+                assert lib.accel_step_harmonic(startr, U, p, q, hw0, out) == 0
+                assert (out[0], out[2]) == (rlo, numrs)
+                assert out[1] == math.ceil(rhi)
+                assert out[3] == rlo - hw0
+                assert out[4] == math.ceil(rhi) + hw0 - (rlo - hw0) + 1
+
+
+def test_harmonic_indices_match_reference_formula(lib):
+    # addPowers (bpd_gpu_kernels.cu:139-153) evaluates these in double precision
+    zmax, numharm, U = 200, 8, 7734
+    geom = O.bank_geometry(zmax, numharm, U)
+    nz = int(geom[0, 3])
+    rind = (C.c_int * U)()
+    zind = (C.c_int * nz)()
+    for startr in (268, 4135, 268 + 3867 * 300):
+        lastr = startr + U // 2 - 0.5
+        for g in geom[1:]:
+            p, q, hw0, zlo_h = int(g[0]), int(g[1]), int(g[5]), int(g[6])
+            rlo, _, _, numrs = O.step_ffdot(p, q, zmax, U, float(startr), lastr)
+            assert lib.accel_harmonic_indices(startr, U, p, q, hw0, -zmax, zlo_h, U, nz,
+                                              rind, zind) == 0
+            f = p / q
+            for i in range(0, U, 7):
+                rr = int(startr) + i * 0.5
+                subr = int(2 * rr * f + 0.5) * 0.5
+                want = int((subr - rlo) * 2) & 0xFFFF
+                assert rind[i] == want
+                assert 0 <= rind[i] < numrs
+            for z in range(nz):
+                zz = -zmax + 2 * z
+                subz = int(zz * f)
+                assert zind[z] == int((subz - zlo_h) * 0.5)
+                assert 0 <= zind[z] < int(g[3])
