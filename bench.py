@@ -335,7 +335,7 @@ def run_ours(args):
     kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / max(sum(x["ms"] for x in k.values()), 1e-9), 4)}
             for name, v in k.items()}
-    cb = cpu_baseline(args.cpu_seconds)
+    cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,

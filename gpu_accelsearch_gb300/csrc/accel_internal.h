@@ -40,6 +40,7 @@ struct SegDesc {
 // Per-harmonic plan of a search: bank data plus plane layout.
 struct HarmPlan {
     int p, q;               // harmnum, maxharm
+    int lq;                 // log2(q) (q is a power of two)
     int M;                  // half segment length
     int hw0, zlo, numzs;
     int wmax;               // columns written per f-dot row (max numrs over steps)

@@ -298,6 +298,8 @@ int build_plan(accel_ctx* c) {
         HarmPlan& P = c->hp[h];
         P.p = b.harmnum;
         P.q = b.maxharm;
+        P.lq = 0;
+        while ((1 << P.lq) < P.q) P.lq++;
         P.M = b.M;
         P.hw0 = b.hw0;
         P.zlo = b.zlo;
@@ -327,6 +329,8 @@ int build_plan(accel_ctx* c) {
     }
     c->dstride = (doff + 31) & ~31LL;
     c->pstride = (poff + 63) & ~63LL;
+    if (c->pstride >= (1LL << 31))
+        return set_err(ACCEL_ERR_UNSUPPORTED, "power planes of one step exceed 2^31 floats");
     c->numzs0 = c->hp[0].numzs;
     c->zlo0 = c->hp[0].zlo;
     // zind must stay inside each harmonic's plane for every fundamental row

@@ -130,46 +130,60 @@ __global__ void __launch_bounds__(M / 16) k_plane(const PlaneArgs a, const float
 }
 
 // ------------------------------------------------------------------ hsum
+// One thread per fundamental column i, kHsumRows f-dot rows per block.  The
+// reference's index arithmetic (twice_required_r, sub_zind) divides by
+// powers of two only, so it is done with shifts here; the per-column
+// sub-harmonic offsets are computed once per thread.
 constexpr int kHsumCols = 128;
-constexpr int kHsumRows = 8;
+constexpr int kHsumRows = 32;
+
+__device__ __forceinline__ long long twice_r_shift(long long r2, int p, int lq) {
+    return (2LL * r2 * p + (1LL << lq)) >> (lq + 1);
+}
+__device__ __forceinline__ int trunc_shift(int x, int k) {  // C division by 2^k
+    return x >= 0 ? (x >> k) : -((-x) >> k);
+}
 
 template <int NH>
 __global__ void __launch_bounds__(kHsumCols) k_hsum(const HsumArgs a) {
     const int i = blockIdx.x * kHsumCols + threadIdx.x;
     const int seg = blockIdx.z;
     const bool valid = i < a.uselen;
-    const SegDesc sd = a.segs[seg];
-    const float* P = a.planes + (long long)seg * a.pstride;
+    const long long startr = a.segs[seg].startr;
+    const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
     const int lane = threadIdx.x & 31;
 
-    int rind[NH];
-    int zl[NH];
+    int roff[NH];
 #pragma unroll
     for (int h = 1; h < NH; h++) {
         const HarmPlan& H = a.h[h];
-        const long long rlo_h = twice_required_r(2 * sd.startr, H.p, H.q) >> 1;
-        rind[h] = valid ? sub_rind(sd.startr, i, H.p, H.q, rlo_h) : 0;
-        zl[h] = H.zlo;
+        const long long rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+        const int rind = (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - rlo2);
+        roff[h] = (int)H.poff + rind;
     }
     const int z0 = blockIdx.y * kHsumRows;
-#pragma unroll 1
-    for (int zr = 0; zr < kHsumRows; zr++) {
-        const int z = z0 + zr;
-        if (z >= a.numzs0) break;
+    const int zend = min(z0 + kHsumRows, a.numzs0);
+    const int base0 = (int)a.h[0].poff + i;
+#pragma unroll 2
+    for (int z = z0; z < zend; z++) {
         const int zz = a.zlo0 + kDz * z;
-        float s = valid ? P[a.h[0].poff + (long long)z * a.h[0].prow + i] : 0.f;
+        float v[NH];
+        v[0] = valid ? P[base0 + z * a.h[0].prow] : 0.f;
+#pragma unroll
+        for (int h = 1; h < NH; h++) {
+            const HarmPlan& H = a.h[h];
+            const int d = trunc_shift(zz * H.p, H.lq) - H.zlo;
+            const int zind = d >= 0 ? (d >> 1) : -((-d) >> 1);
+            v[h] = valid ? P[roff[h] + zind * H.prow] : 0.f;
+        }
+        float s = 0.f;
 #pragma unroll
         for (int h = 0; h < NH; h++) {
-            if (h > 0) {
-                const HarmPlan& H = a.h[h];
-                const int zind = sub_zind(zz, H.p, H.q, zl[h]);
-                if (valid) s += P[H.poff + (long long)zind * H.prow + rind[h]];
-            }
+            s = (h == 0) ? v[0] : s + v[h];
             const int st = a.stage_of[h];
             if (st >= 0) {
-                if (a.stage_out)
-                    if (valid)
-                        a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
+                if (a.stage_out && valid)
+                    a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
                 const bool hit = valid && s > a.cut[st];
                 const unsigned m = __ballot_sync(0xffffffffu, hit);
                 if (m) {
