@@ -108,6 +108,9 @@ int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
 
+// Record an error message for accel_last_error() and return `code`.
+int set_error(int code, const char* fmt, ...);
+
 // whitening
 struct WhitenPlan;
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,

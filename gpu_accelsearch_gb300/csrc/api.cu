@@ -609,6 +609,18 @@ void free_ctx(accel_ctx* c) {
 
 }  // namespace
 
+namespace accel {
+int set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+}  // namespace accel
+
 // =================================================================== C ABI
 extern "C" {
 

@@ -11,6 +11,10 @@
 //                     from its two neighbouring blocks, then the scaling
 //                     with the reference's float arithmetic.
 // Results are bit-identical to the reference's host routine.
+#include <cmath>
+#include <mutex>
+
+#include "../../include/accelsearch.h"
 #include "accel_internal.h"
 
 namespace accel {
@@ -90,3 +94,100 @@ int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d
 }
 
 }  // namespace accel
+
+// --------------------------------------------------------------------------
+// Allocation-free whitening (accel_whiten_noalloc).
+//
+// Same kernels as above; their scratch -- the block table (start, length)
+// and the per-block levels -- lives in one file-scope device array instead
+// of memory allocated by a context.  Every GPU that loads the library holds
+// this array (2 MiB) until the process exits.  All calls share it, so calls
+// whose GPU work overlaps race; every byte a call reads is written earlier
+// by the same call (table copy, then medians), so nothing needs clearing.
+namespace accel {
+namespace {
+
+constexpr int kNoAllocBlocks = 131072;
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocBlocks * (2 * sizeof(int) + sizeof(double));
+static __device__ __align__(256) unsigned char g_whiten_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNoAllocDevices];           // device address of g_whiten_scratch
+int g_noalloc_start[kNoAllocBlocks];             // host staging of the block table
+int g_noalloc_len[kNoAllocBlocks];
+
+// The block recurrence of deredden (bpd_noise.c:33-79) into fixed arrays.
+// Returns the number of blocks, or -1 when it exceeds kNoAllocBlocks.
+int plan_blocks_fixed(unsigned numbins, int initbuf, int maxbuf) {
+    int n = 0, binnum = 1, buflen = initbuf;
+    g_noalloc_start[n] = binnum;
+    g_noalloc_len[n++] = buflen;
+    binnum += buflen;
+    buflen = (int)(initbuf * std::log((double)binnum));
+    if (buflen > maxbuf) buflen = maxbuf;
+    while ((unsigned)(binnum + buflen) < numbins) {
+        if (n >= kNoAllocBlocks) return -1;
+        g_noalloc_start[n] = binnum;
+        g_noalloc_len[n++] = buflen;
+        binnum += buflen;
+        buflen = (int)(initbuf * std::log((double)binnum));
+        if (buflen > maxbuf) buflen = maxbuf;
+    }
+    return n;
+}
+
+}  // namespace
+}  // namespace accel
+
+extern "C" int accel_whiten_noalloc(accel_complex* spec, long long numbins, int initbuf, int maxbuf,
+                                    void* stream) {
+    using namespace accel;
+    if (!spec) return set_error(ACCEL_ERR_INVALID, "accel_whiten_noalloc: null spectrum");
+    if (initbuf < 1 || maxbuf < 1 || maxbuf > 49152)
+        return set_error(ACCEL_ERR_INVALID,
+                         "accel_whiten_noalloc: block widths must be in [1, 49152]");
+    if (numbins <= 1 + (long long)initbuf || numbins > 0xffffffffLL)
+        return set_error(ACCEL_ERR_INVALID, "accel_whiten_noalloc: %lld bins out of range", numbins);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return set_error(ACCEL_ERR_CUDA, "accel_whiten_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoAllocDevices)
+        return set_error(ACCEL_ERR_UNSUPPORTED, "accel_whiten_noalloc: device %d", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        // once per device, with that device current: the array's device address
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_whiten_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(ACCEL_ERR_CUDA, "accel_whiten_noalloc: cudaGetSymbolAddress: %s",
+                             cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    const int nb = plan_blocks_fixed((unsigned)numbins, initbuf, maxbuf);
+    if (nb < 0)
+        return set_error(ACCEL_ERR_INVALID,
+                         "accel_whiten_noalloc: %lld bins need more than %d whitening blocks, the "
+                         "size of the static scratch (about 1.2e7 bins with the default widths)",
+                         numbins, kNoAllocBlocks);
+    int maxlen = 0;
+    for (int i = 0; i < nb; i++) maxlen = g_noalloc_len[i] > maxlen ? g_noalloc_len[i] : maxlen;
+    char* base = static_cast<char*>(g_noalloc_addr[dev]);
+    int* d_start = reinterpret_cast<int*>(base);
+    int* d_len = reinterpret_cast<int*>(base + sizeof(int) * kNoAllocBlocks);
+    double* d_med = reinterpret_cast<double*>(base + 2 * sizeof(int) * kNoAllocBlocks);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // pageable source: the copies have left the host arrays when they return
+    e = cudaMemcpyAsync(d_start, g_noalloc_start, sizeof(int) * nb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_len, g_noalloc_len, sizeof(int) * nb, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess)
+        return set_error(ACCEL_ERR_CUDA, "accel_whiten_noalloc: block table copy: %s",
+                         cudaGetErrorString(e));
+    if (launch_whiten(d_start, d_len, nb, d_med, reinterpret_cast<float2*>(spec), (unsigned)numbins,
+                      maxlen, st) != 0)
+        return set_error(ACCEL_ERR_CUDA, "accel_whiten_noalloc: launch: %s",
+                         cudaGetErrorString(cudaGetLastError()));
+    return ACCEL_OK;
+}

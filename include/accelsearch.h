@@ -141,6 +141,23 @@ int  accel_candidates(accel_ctx *ctx, accel_candidate *out, long long cap, long 
 /* ------------------------------------------------------------ stage calls */
 /* Whitening in place (deredden, bpd_noise.c:12-92). */
 int  accel_whiten(accel_ctx *ctx, accel_complex *spec_dev, long long numbins);
+/* Whitening in place, like accel_whiten, for callers that cannot allocate
+ * device memory.  No counterpart in the reference.  Some hosts forbid
+ * cudaMalloc on the data path: a real-time pipeline that sizes all memory at
+ * start-up (cudaMalloc synchronises the device and can fail under memory
+ * pressure mid-observation), or a plugin running inside another
+ * application's memory pool or under a hard device-memory limit.  This entry
+ * point needs no context and calls no cudaMalloc, cudaFree or other
+ * allocating routine: its scratch is a static 2 MiB device array that every
+ * GPU loading the library holds until exit, enough for 131072 whitening
+ * blocks (about 1.2e7 bins with the default widths 6/200); larger spectra
+ * are rejected with ACCEL_ERR_INVALID.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the array: calls whose GPU
+ * work overlaps race, so serialise them (one stream, or synchronise).
+ * cuda_stream may be NULL (the legacy default stream). */
+int  accel_whiten_noalloc(accel_complex *spec_dev, long long numbins, int initbuf, int maxbuf,
+                          void *cuda_stream);
 /* Real-to-complex FFT of a device series into spec_dev (n/2+1 bins). */
 int  accel_rfft(accel_ctx *ctx, const float *series_dev, long long n, accel_complex *spec_dev);
 /* Segment spectra of nseg steps (first bins startr[]): per step and
