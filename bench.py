@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--trials", type=int, default=256, help="DM trials per GPU")
     ap.add_argument("--chunk", type=int, default=0, help="segments per launch group (0: auto)")
+    ap.add_argument("--fftlen", type=int, default=0,
+                    help="segment length; 0: chosen by the autotuner among 4096/8192/16384")
+    ap.add_argument("--split", type=int, default=-1, help="plane kernel layout (-1: autotuner)")
+    ap.add_argument("--tuning", default="", help="JSON of extra accel_tuning fields to apply")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -202,12 +206,12 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic():
-    """DRAM bytes per segment of the plane kernel from the committed ncu
-    summary (profiles/plane_kernel_traffic.json), or None."""
+def load_traffic(kernel: str):
+    """DRAM bytes per segment of a kernel from the committed ncu summary
+    (profiles/dram_traffic_per_segment.json), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "plane_kernel_traffic.json")) as f:
-            return float(json.load(f)["dram_bytes_per_segment"])
+        with open(os.path.join(ROOT, "profiles", "dram_traffic_per_segment.json")) as f:
+            return float(json.load(f)[kernel]["dram_bytes_per_segment"])
     except Exception:
         return None
 
@@ -229,15 +233,28 @@ def run_ours(args):
     lengths, sigs = make_batch(args.trials, seed=1000 + rank)
     series = device_series(torch, lengths, sigs, seed=2000 + rank)
     ptrs = [x.data_ptr() for x in series]
-    s = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=args.chunk,
-                    device=local)
+    from gpu_accelsearch_gb300.search import autotune
+    tuned = None
+    if args.fftlen == 0 or args.chunk == 0 or args.split < 0:
+        fl = (4096, 8192, 16384) if args.fftlen == 0 else (args.fftlen,)
+        kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=96, device=local)
+        tuned = {"fftlen": kw["fftlen"], "chunk_segments": tun["chunk_segments"],
+                 "plane_split": tun["plane_split"], "fused_sum": tun["fused_sum"],
+                 "sample_cells_per_s": rate}
+    fftlen = args.fftlen or tuned["fftlen"]
+    chunk = args.chunk or tuned["chunk_segments"]
+    split = args.split if args.split >= 0 else tuned["plane_split"]
+    s = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local)
+    extra = json.loads(args.tuning) if args.tuning else {}
+    if tuned and "fused_sum" not in extra:
+        extra["fused_sum"] = tuned["fused_sum"]
+    s.set_tuning(chunk_segments=chunk, plane_split=split, **extra)
     U, nz0 = s.uselen, s.harmonics[0].numzs
     nseg = sum(s.step_count(n, DT) for n in lengths)
     cells = nseg * U * nz0
-    plane_cells = 0
-    for h in s.harmonics:  # mean row width over the step phases ~ plane_width - 1
-        plane_cells += h.numzs * (U if h.harmnum == h.maxharm == 1 else h.plane_width - 1)
-    bytes_per_cell = 8.0 * plane_cells / (U * nz0)
+    # plane cells per segment (mean row width over the step phases ~ plane_width - 1)
+    sub_cells = sum(h.numzs * (h.plane_width - 1) for h in s.harmonics[1:])
+    bytes_per_cell = 8.0 * (sub_cells + U * nz0) / (U * nz0)
 
     for _ in range(args.warmup):
         s.search(ptrs, DT, on_device=True, nsamples=lengths)
@@ -260,7 +277,8 @@ def run_ours(args):
     barrier()
     st = s.stats()
     s.profile(False)
-    el_t = torch.tensor([el], device="cuda")
+    wall = el
+    el_t = torch.tensor([st["search_ms"] / 1e3], device="cuda")  # CUDA-event device time
     if world > 1:
         dist.all_reduce(el_t, op=dist.ReduceOp.MAX)
     el = float(el_t.item())
@@ -274,12 +292,12 @@ def run_ours(args):
         s.search_ptrs(hptrs, lengths, DT, on_device=False)  # warm
         barrier()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        s.reset_stats()
         nc = 0
         for _ in range(args.steps):
             nc = s.search_ptrs(hptrs, lengths, DT, on_device=False)
         torch.cuda.synchronize()
-        el2 = time.perf_counter() - t0
+        el2 = s.stats()["search_ms"] / 1e3
         barrier()
         el2_t = torch.tensor([el2], device="cuda")
         if world > 1:
@@ -296,13 +314,13 @@ def run_ours(args):
         pn = p.step_count(1 << 22, DT)
         p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        p.reset_stats()
         reps = 3
         for _ in range(reps):
             p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
         torch.cuda.synchronize()
-        pel = time.perf_counter() - t0
-        plain = {"value": pn * U * nz0 * reps / pel, "unit": "cells/s",
+        pel = p.stats()["search_ms"] / 1e3
+        plain = {"value": pn * p.uselen * p.harmonics[0].numzs * reps / pel, "unit": "cells/s",
                  "workload": "one 2^22-sample trial, one overlap-save step per launch group "
                              f"({pn} steps)"}
         p.close()
@@ -315,38 +333,61 @@ def run_ours(args):
 
     peak, peak_kind = load_peaks()
     k = st["kinds"]
-    plane_ms = k["plane"]["ms"]
-    plane_launches = max(k["plane"]["launches"], 1)
-    seg_per_launch = st["segments"] / max(k["hsum"]["launches"], 1)
-    # algorithmic bytes of the plane kernel: each plane cell written once (4 B)
-    plane_bytes = 0.5 * bytes_per_cell * st["cells"]
-    achieved = plane_bytes / (plane_ms / 1e3) / 1e9 if plane_ms > 0 else None
-    tr = load_traffic()
-    roofline = {"bound": "hbm", "kernel": "k_plane (fused correlate + inverse FFT + |X|^2)",
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None,
-                "peak_source": peak_kind,
-                "algorithmic_bytes_per_cell": 0.5 * bytes_per_cell,
-                "traffic": (tr * st["segments"] / plane_launches) if tr else None,
-                "note": "achieved = 4 B per plane cell written / CUDA-event time of the "
-                        "plane launches in the timed region"}
-    step_roofline = {"bytes_per_cell": bytes_per_cell, "achieved": value * bytes_per_cell / 1e9,
-                     "peak": peak, "unit": "GB/s", "frac": value * bytes_per_cell / 1e9 / peak}
+    # algorithmic bytes per kernel: k_plane writes each plane cell it
+    # produces once (4 B); k_hsum reads every plane cell once (4 B); in the
+    # fused layout k_fund_sum reads the sub-harmonic cells once and the
+    # fundamental plane never leaves the chip.
+    segs = st["segments"]
+    fused = s.tuning()["fused_sum"]
+    fund_cells = U * nz0
+    cells_by_kind = {"plane": sub_cells + (0 if fused else fund_cells),
+                     "hsum": sub_cells + fund_cells, "fund": sub_cells}
+    per_kernel = {}
+    for name in ("plane", "hsum", "fund"):
+        ms = k[name]["ms"]
+        if ms > 0:
+            b = 4.0 * cells_by_kind[name] * segs
+            per_kernel[name] = {"launches": k[name]["launches"], "ms": ms,
+                                "bytes_per_launch": b / max(k[name]["launches"], 1),
+                                "achieved": b / (ms / 1e3) / 1e9}
+    dom = max(per_kernel, key=lambda n: per_kernel[n]["ms"]) if per_kernel else None
+    names = {"plane": "k_plane (correlate + inverse FFT + |X|^2 power planes)",
+             "hsum": "k_hsum_tile (harmonic sum + threshold over shared-memory tiles)",
+             "fund": "k_fund_sum (fundamental plane fused with harmonic sum + threshold)"}
+    tr = load_traffic(dom) if dom else None
+    roofline = None
+    if dom:
+        pk = per_kernel[dom]
+        roofline = {"bound": "hbm", "kernel": names[dom], "achieved": pk["achieved"], "peak": peak,
+                    "unit": "GB/s", "frac": pk["achieved"] / peak, "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": pk["bytes_per_launch"],
+                    "traffic": (tr * segs / max(pk["launches"], 1)) if tr else None,
+                    "note": "achieved = algorithmic bytes (4 B per plane cell moved) per launch / "
+                            "mean CUDA-event time of its launches in the timed region",
+                    "per_kernel": {n: {"achieved_GBs": round(v["achieved"], 1),
+                                       "frac": round(v["achieved"] / peak, 4)}
+                                   for n, v in per_kernel.items()}}
+    step_roofline = {"bytes_per_cell": bytes_per_cell,
+                     "achieved": value / world * bytes_per_cell / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": value / world * bytes_per_cell / 1e9 / peak,
+                     "note": "every plane written once and read once per fundamental cell"}
+    tot_ms = max(sum(x["ms"] for x in k.values()), 1e-9)
     kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
-                   "share": round(v["ms"] / max(sum(x["ms"] for x in k.values()), 1e-9), 4)}
-            for name, v in k.items()}
+                   "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
     cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "wall_ms_per_step": 1e3 * wall / args.steps, "timing": "CUDA events on the library stream, "
+        "first input copy to last candidate read-back; max over ranks",
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded N(0,1) float32 series (torch Philox), 10% with one "
                 "injected accelerated sinusoid",
         "config": {"workload": f"batched: {args.trials} DM trials per GPU, lengths uniform in "
                                "{2^20, 2^21, 2^22, 3*2^20}, dt=64us, zmax=200, 8 harmonics, "
-                               f"L=8192 (uselen {U}), sigma=6",
+                               f"L={fftlen} (uselen {U}) chosen by the autotuner, sigma=6",
                    "segments_per_step": nseg, "cells_per_step": cells,
-                   "chunk_segments": s.config.chunk_segments or "auto",
+                   "fftlen": fftlen, "uselen": U, "tuning": s.tuning(), "autotuner": tuned,
                    "l2": f"inputs ({sum(lengths) * 4 / 1e9:.2f} GB of series per GPU) larger "
                          "than L2; no flush",
                    "parallelism": f"trial-sharded replicas x{world}"},

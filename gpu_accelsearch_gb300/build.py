@@ -21,9 +21,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libaccelsearch.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "bank.cu", "search.cu", "whiten.cu"]
+SOURCES = ["api.cu", "bank.cu", "search.cu", "search_plane_lo.cu", "search_plane_hi.cu",
+           "search_fund_lo.cu", "search_fund_hi.cu", "tune.cu", "whiten.cu"]
 EXTRA = {"bank.cu": ["-fmad=false"]}
-HEADERS = ["accel_common.cuh", "accel_internal.h", "fft_smem.cuh"]
+HEADERS = ["accel_common.cuh", "accel_internal.h", "fft_smem.cuh", "search_kernels.cuh"]
 
 
 def nvcc() -> str:

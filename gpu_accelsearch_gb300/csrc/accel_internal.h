@@ -71,6 +71,7 @@ struct PlaneArgs {
     float* planes;          // [nseg][pstride]
     long long pstride;
     int use_fp16;
+    int split;              // 1: even/odd transforms on separate threads
 };
 
 // Raw candidate as written by the harmonic-sum kernel (16 bytes).
@@ -100,13 +101,42 @@ struct HsumArgs {
     int nstages;
 };
 
+// Fundamental plane fused with the harmonic sum (k_fund_sum).
+struct FundArgs {
+    HarmPlan h[kMaxHarm];   // all harmonics, bank order
+    int nh;
+    const float2* dbuf;
+    long long dstride;
+    const float* planes;    // sub-harmonic planes of the group
+    long long pstride;
+    int use_fp16;
+    int split;
+    int uselen;
+    int numzs0, zlo0;
+    int stage_of[kMaxHarm];
+    float cut[kMaxStages];
+    const SegDesc* segs;
+    RawCand* cands;
+    unsigned long long* ncand;
+    long long cap;
+    int seg_base;
+    float* stage_out;       // optional [nseg][nstages][numzs0][uselen]
+    int nstages;
+};
+
 // ---- launchers (return 0 or -1 after a launch error) ----
+int launch_fund_sum(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_twiddles(float2* tw, cudaStream_t st);
 int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int nh, int ntpl,
                       float2* resp, int rstride, bool fp16, cudaStream_t st);
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
+int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st);
+// Tile geometry of launch_hsum_tile (the host proves the shared-memory bound).
+constexpr int kHsumTileZ = 16;
+constexpr int kHsumTileI = 256;
+constexpr int kHsumTileFloats = 15360;
 
 // Record an error message for accel_last_error() and return `code`.
 int set_error(int code, const char* fmt, ...);

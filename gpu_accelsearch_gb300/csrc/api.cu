@@ -144,6 +144,15 @@ struct accel_ctx {
 
     // work buffers
     int chunk = 1;
+    int plane_split = 0;
+    int fused_sum = 0;
+    int overlap = 1;          // sum of group k on stream2 while group k+1 is transformed
+    cudaStream_t stream2 = nullptr;
+    float* planes2 = nullptr; // second plane buffer for the overlap
+    cudaEvent_t ev_fork = nullptr, ev_plane[2] = {nullptr, nullptr}, ev_sum[2] = {nullptr, nullptr};
+    bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
+    int hsum_tiled = 1;
+    int tile_floats = 0;
     float2* dbuf = nullptr;
     float* planes = nullptr;
     SegDesc* d_segs = nullptr;
@@ -167,6 +176,7 @@ struct accel_ctx {
     std::vector<Ev> pending;
     std::vector<cudaEvent_t> evpool;
     accel_stats stats{};
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // bracket each search call
 };
 
 namespace {
@@ -176,7 +186,7 @@ int ensure_device(accel_ctx* c) {
     return ACCEL_OK;
 }
 
-enum { K_PREP = 0, K_PLANE = 1, K_HSUM = 2, K_WHITEN = 3, K_RFFT = 4 };
+enum { K_PREP = 0, K_PLANE = 1, K_HSUM = 2, K_WHITEN = 3, K_RFFT = 4, K_FUND = 5 };
 
 cudaEvent_t take_event(accel_ctx* c) {
     cudaEvent_t e = nullptr;
@@ -193,19 +203,21 @@ cudaEvent_t take_event(accel_ctx* c) {
 struct ProfScope {
     accel_ctx* c;
     int kind;
+    cudaStream_t st;
     cudaEvent_t a = nullptr;
-    ProfScope(accel_ctx* c_, int kind_, int nlaunch) : c(c_), kind(kind_) {
+    ProfScope(accel_ctx* c_, int kind_, int nlaunch, cudaStream_t st_ = nullptr)
+        : c(c_), kind(kind_), st(st_ ? st_ : c_->stream) {
         if (kind != K_RFFT) c->stats.launches += nlaunch;
         c->stats.kind_launches[kind] += nlaunch;
         if (c->profiling) {
             a = take_event(c);
-            cudaEventRecord(a, c->stream);
+            cudaEventRecord(a, st);
         }
     }
     ~ProfScope() {
         if (a) {
             cudaEvent_t b = take_event(c);
-            cudaEventRecord(b, c->stream);
+            cudaEventRecord(b, st);
             c->pending.push_back({kind, a, b});
         }
     }
@@ -347,6 +359,42 @@ int build_plan(accel_ctx* c) {
             c->mvals.push_back(c->hp[h].M);
     for (int s = 0; s < c->nstages; s++)
         c->cuts[s] = (float)power_cut(c->cfg.sigma, 1 << s, c->cfg.numindep);
+    // Largest shared-memory footprint of a k_hsum_tile tile, over every tile
+    // position and every step phase (the geometry repeats with period q in
+    // startr), with the kernel's own index arithmetic.
+    int worst = 0, qmax = 1;
+    for (int h = 0; h < c->nh; h++) qmax = std::max(qmax, c->hp[h].q);
+    for (long long ph = 0; ph < 4LL * qmax; ph++) {
+        const long long startr = 1000000 + ph;
+        for (int z0 = 0; z0 < c->numzs0; z0 += kHsumTileZ) {
+            const int nz = std::min(kHsumTileZ, c->numzs0 - z0);
+            for (int i0 = 0; i0 < U; i0 += kHsumTileI) {
+                const int ni = std::min(kHsumTileI, U - i0);
+                int off = 0;
+                for (int h = 0; h < c->nh; h++) {
+                    const HarmPlan& H = c->hp[h];
+                    int rfirst = i0, rlast = i0 + ni - 1, zf = z0, zl = z0 + nz - 1;
+                    if (h > 0) {
+                        const long long rlo = twice_required_r(2 * startr, H.p, H.q) >> 1;
+                        rfirst = sub_rind(startr, i0, H.p, H.q, rlo);
+                        rlast = sub_rind(startr, i0 + ni - 1, H.p, H.q, rlo);
+                        zf = sub_zind(c->zlo0 + kDz * z0, H.p, H.q, H.zlo);
+                        zl = sub_zind(c->zlo0 + kDz * (z0 + nz - 1), H.p, H.q, H.zlo);
+                    }
+                    const int c0 = rfirst & ~3;
+                    const int w4 = ((rlast - c0) >> 2) + 1;
+                    if (zl < zf || rlast < rfirst || zf < 0 || zl >= H.numzs || (rlast | 3) >= H.prow) {
+                        off = 1 << 30;  // never use the tiled kernel for this plan
+                        break;
+                    }
+                    off += 4 * (zl - zf + 1) * w4;
+                }
+                worst = std::max(worst, off);
+            }
+        }
+    }
+    c->tile_floats = worst;
+    c->tile_ok = worst <= kHsumTileFloats;
     return ACCEL_OK;
 }
 
@@ -359,6 +407,13 @@ int alloc_work(accel_ctx* c) {
     c->chunk = chunk;
     CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * chunk));
     CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * chunk));
+    CK(cudaMalloc(&c->planes2, sizeof(float) * c->pstride * chunk));
+    CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    for (int b = 0; b < 2; b++) {
+        CK(cudaEventCreateWithFlags(&c->ev_plane[b], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_sum[b], cudaEventDisableTiming));
+    }
     c->cand_cap = c->cfg.cand_capacity > 0 ? c->cfg.cand_capacity : (1LL << 22);
     CK(cudaMalloc(&c->d_cands, sizeof(RawCand) * c->cand_cap));
     CK(cudaMalloc(&c->d_ncand, sizeof(unsigned long long)));
@@ -436,44 +491,79 @@ int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec) {
 }
 
 // Launch one group of nseg prepared segment descriptors (device array).
+// fused: the fundamental's plane is not stored; k_fund_sum adds the
+// sub-harmonic planes to it row by row (the search path).  Otherwise every
+// plane is stored and, with do_sum, k_hsum sums them (the stage API).
 int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float* stage_out,
-              const float2* dh_in, float* planes_out, bool do_prep, bool do_plane, bool do_sum) {
+              const float2* dh_in, float* planes_out, bool do_prep, bool do_plane, bool do_sum,
+              bool fused = false, cudaStream_t sum_stream = nullptr) {
+    if (!sum_stream) sum_stream = c->stream;
     float2* dbuf = dh_in ? const_cast<float2*>(dh_in) : c->dbuf;
     float* planes = planes_out ? planes_out : c->planes;
     for (int M : c->mvals) {
         PrepArgs pa{};
         PlaneArgs la{};
-        int k = 0, zb = 0;
+        int k = 0, kp = 0, zb = 0;
         for (int h = 0; h < c->nh; h++) {
             if (c->hp[h].M != M) continue;
-            pa.h[k] = c->hp[h];
-            la.h[k] = c->hp[h];
-            la.h[k].zbase = zb;
+            pa.h[k++] = c->hp[h];
+            if (fused && h == 0) continue;
+            la.h[kp] = c->hp[h];
+            la.h[kp].zbase = zb;
             zb += c->hp[h].numzs;
-            k++;
+            kp++;
         }
         pa.nh = k;
         pa.uselen = c->uselen;
         pa.segs = d_segs;
         pa.dbuf = dbuf;
         pa.dstride = c->dstride;
-        la.nh = k;
+        la.nh = kp;
         la.ntpl = zb;
         la.dbuf = dbuf;
         la.dstride = c->dstride;
         la.planes = planes;
         la.pstride = c->pstride;
         la.use_fp16 = c->cfg.template_fp16;
+        la.split = c->plane_split;
         if (do_prep) {
             ProfScope ps(c, K_PREP, 1);
             CKL(launch_prep(M, pa, nseg, c->tw, c->stream), "segment preparation");
         }
-        if (do_plane) {
+        if (do_plane && kp > 0) {
             ProfScope ps(c, K_PLANE, 1);
             CKL(launch_plane(M, la, nseg, c->tw, c->stream), "power plane");
         }
     }
-    if (do_sum) {
+    if (fused) {
+        FundArgs fa{};
+        for (int h = 0; h < c->nh; h++) {
+            fa.h[h] = c->hp[h];
+            fa.stage_of[h] = c->stage_of[h];
+        }
+        fa.nh = c->nh;
+        fa.dbuf = dbuf;
+        fa.dstride = c->dstride;
+        fa.planes = planes;
+        fa.pstride = c->pstride;
+        fa.use_fp16 = c->cfg.template_fp16;
+        fa.split = c->plane_split;
+        fa.uselen = c->uselen;
+        fa.numzs0 = c->numzs0;
+        fa.zlo0 = c->zlo0;
+        for (int s = 0; s < c->nstages; s++) fa.cut[s] = c->cuts[s];
+        fa.segs = d_segs;
+        fa.cands = c->d_cands;
+        fa.ncand = c->d_ncand;
+        fa.cap = c->cand_cap;
+        fa.seg_base = seg_base;
+        fa.stage_out = stage_out;
+        fa.nstages = c->nstages;
+        ProfScope ps(c, K_FUND, 1);
+        c->stats.segments += nseg;
+        c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
+        CKL(launch_fund_sum(fa, nseg, c->tw, c->stream), "fundamental plane and harmonic sum");
+    } else if (do_sum) {
         HsumArgs ha{};
         for (int h = 0; h < c->nh; h++) {
             ha.h[h] = c->hp[h];
@@ -493,10 +583,13 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ha.seg_base = seg_base;
         ha.stage_out = stage_out;
         ha.nstages = c->nstages;
-        ProfScope ps(c, K_HSUM, 1);
+        ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
-        CKL(launch_hsum(ha, nseg, c->stream), "harmonic sum");
+        if (c->tile_ok && c->hsum_tiled)
+            CKL(launch_hsum_tile(ha, nseg, sum_stream), "harmonic sum (tiled)");
+        else
+            CKL(launch_hsum(ha, nseg, sum_stream), "harmonic sum");
     }
     return ACCEL_OK;
 }
@@ -533,21 +626,56 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
     if (total > 0)
         CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
                            c->stream));
-    for (long long g = 0; g < total; g += c->chunk) {
+    const bool overlap = c->overlap && !c->fused_sum && c->planes2 && c->stream2;
+    if (overlap) {
+        // fork: stream2 starts after everything queued so far on the main stream
+        CK(cudaEventRecord(c->ev_fork, c->stream));
+        CK(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+    }
+    for (long long g = 0, k = 0; g < total; g += c->chunk, k++) {
         int n = (int)std::min<long long>(c->chunk, total - g);
-        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true);
+        if (!overlap) {
+            rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true,
+                           c->fused_sum != 0);
+            if (rc) return rc;
+            continue;
+        }
+        // group k: planes into buffer k%2 on the main stream, summed on stream2
+        const int b = (int)(k & 1);
+        float* pb = b ? c->planes2 : c->planes;
+        if (k >= 2) CK(cudaStreamWaitEvent(c->stream, c->ev_sum[b], 0));  // buffer b free again
+        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, true, true, false);
         if (rc) return rc;
+        CK(cudaEventRecord(c->ev_plane[b], c->stream));
+        CK(cudaStreamWaitEvent(c->stream2, c->ev_plane[b], 0));
+        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, false, false, true, false,
+                       c->stream2);
+        if (rc) return rc;
+        CK(cudaEventRecord(c->ev_sum[b], c->stream2));
+    }
+    if (overlap) {
+        // join: the main stream continues after the last sum
+        CK(cudaEventRecord(c->ev_fork, c->stream2));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_fork, 0));
     }
     CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    prof_collect(c);
     unsigned long long nraw = *c->h_ncand;
     c->last_raw = nraw;
     long long keep = (long long)std::min<unsigned long long>(nraw, (unsigned long long)c->cand_cap);
     std::vector<RawCand> raw(keep);
     if (keep > 0)
-        CK(cudaMemcpy(raw.data(), c->d_cands, sizeof(RawCand) * keep, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(raw.data(), c->d_cands, sizeof(RawCand) * keep, cudaMemcpyDeviceToHost,
+                           c->stream));
+    CK(cudaEventRecord(c->ev_end, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end) == cudaSuccess) c->stats.search_ms += ms;
+        c->stats.searches++;
+    }
+    prof_collect(c);
     c->results.clear();
     c->results.reserve(keep);
     for (const RawCand& r : raw) {
@@ -584,6 +712,8 @@ void free_ctx(accel_ctx* c) {
         cudaEventDestroy(e.b);
     }
     for (auto e : c->evpool) cudaEventDestroy(e);
+    if (c->ev_begin) cudaEventDestroy(c->ev_begin);
+    if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (auto& kv : c->wplans) {
         cudaFree(kv.second.d_start);
         cudaFree(kv.second.d_len);
@@ -598,6 +728,13 @@ void free_ctx(accel_ctx* c) {
     cudaFree(c->tw);
     cudaFree(c->dbuf);
     cudaFree(c->planes);
+    cudaFree(c->planes2);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    for (int b = 0; b < 2; b++) {
+        if (c->ev_plane[b]) cudaEventDestroy(c->ev_plane[b]);
+        if (c->ev_sum[b]) cudaEventDestroy(c->ev_sum[b]);
+    }
     cudaFree(c->d_segs);
     cudaFreeHost(c->h_segs);
     cudaFree(c->d_cands);
@@ -675,6 +812,8 @@ int accel_create(const accel_config* cfg, accel_ctx** out) {
         if (e != cudaSuccess) rc = set_err(ACCEL_ERR_NOMEM, "twiddles: %s", cudaGetErrorString(e));
         else if (launch_twiddles(c->tw, c->stream) != 0) rc = set_err(ACCEL_ERR_CUDA, "twiddle launch");
     }
+    if (!rc && (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess))
+        rc = set_err(ACCEL_ERR_CUDA, "event creation failed");
     if (!rc) rc = build_bank(c);
     if (!rc) rc = build_plan(c);
     if (!rc) rc = alloc_work(c);
@@ -711,6 +850,7 @@ int accel_set_stream(accel_ctx* c, void* s) {
 int accel_synchronize(accel_ctx* c) {
     if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
     CK(cudaStreamSynchronize(c->stream));
+    if (c->stream2) CK(cudaStreamSynchronize(c->stream2));
     return ACCEL_OK;
 }
 
@@ -733,6 +873,44 @@ int accel_reset_stats(accel_ctx* c) {
     CK(cudaStreamSynchronize(c->stream));
     prof_collect(c);
     c->stats = accel_stats{};
+    return ACCEL_OK;
+}
+
+int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
+    if (!c || !t) return set_err(ACCEL_ERR_INVALID, "null argument");
+    std::memset(t, 0, sizeof(*t));
+    t->chunk_segments = c->chunk;
+    t->plane_split = c->plane_split;
+    t->fused_sum = c->fused_sum;
+    t->hsum_rowwise = !c->hsum_tiled;
+    t->serial_sum = !c->overlap;
+    return ACCEL_OK;
+}
+
+int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
+    if (!c || !t) return set_err(ACCEL_ERR_INVALID, "null argument");
+    if (t->chunk_segments < 1 || t->chunk_segments > 65535)
+        return set_err(ACCEL_ERR_INVALID, "chunk_segments must be in [1, 65535]");
+    int rc = ensure_device(c);
+    if (rc) return rc;
+    c->plane_split = t->plane_split != 0;
+    c->fused_sum = t->fused_sum != 0;
+    c->hsum_tiled = t->hsum_rowwise == 0;
+    c->overlap = t->serial_sum == 0;
+    if (t->chunk_segments != c->chunk) {
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaStreamSynchronize(c->stream2));
+        cudaFree(c->dbuf);
+        cudaFree(c->planes);
+        cudaFree(c->planes2);
+        c->dbuf = nullptr;
+        c->planes = nullptr;
+        c->planes2 = nullptr;
+        c->chunk = t->chunk_segments;
+        CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * c->chunk));
+        CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * c->chunk));
+        CK(cudaMalloc(&c->planes2, sizeof(float) * c->pstride * c->chunk));
+    }
     return ACCEL_OK;
 }
 
@@ -820,6 +998,7 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
     int rc = ensure_device(c);
     if (rc) return rc;
     if ((int)c->trials.size() < ntrials) c->trials.resize(ntrials);
+    CK(cudaEventRecord(c->ev_begin, c->stream));
     std::vector<float2*> specs(ntrials);
     std::vector<long long> nb(ntrials), rlo(ntrials);
     for (int i = 0; i < ntrials; i++) {
@@ -861,6 +1040,7 @@ int accel_search_spectra(accel_ctx* c, int ntrials, const accel_complex* const* 
         return set_err(ACCEL_ERR_INVALID, "bad argument");
     int rc = ensure_device(c);
     if (rc) return rc;
+    CK(cudaEventRecord(c->ev_begin, c->stream));
     std::vector<float2*> specs(ntrials);
     for (int i = 0; i < ntrials; i++) specs[i] = (float2*)wspec[i];
     rc = run_search(c, ntrials, specs.data(), numbins, rlo);
@@ -925,6 +1105,8 @@ int accel_power_planes(accel_ctx* c, const accel_complex* dhalf, int nseg, float
 int accel_sum_harmonics(accel_ctx* c, const float* planes, const long long* startr, int nseg,
                         float* stage_out, long long* ncand) {
     if (!c || !planes || !startr || nseg <= 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    if (reinterpret_cast<uintptr_t>(planes) & 15)
+        return set_err(ACCEL_ERR_INVALID, "planes must be 16-byte aligned");
     int rc = ensure_device(c);
     if (!rc) rc = stage_segs(c, nullptr, 0, startr, nseg);
     if (!rc) CK(cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), c->stream));

@@ -141,11 +141,48 @@ __device__ __forceinline__ void apply_twiddles(float2* v, const float2* __restri
     }
 }
 
+// Base twiddles W^k, W^2k, W^4k, W^8k of one radix-16 pass, loaded ahead of
+// time so that the table lookups are off the pass's critical path.
+struct Tw16 {
+    float2 w1, w2, w4, w8;
+};
+template <int DIR>
+__device__ __forceinline__ Tw16 load_tw16(const float2* __restrict__ tw, int k, int NR) {
+    const int base = k * (kTwN / NR);
+    Tw16 r;
+    r.w1 = twid<DIR>(tw, base);
+    r.w2 = twid<DIR>(tw, 2 * base);
+    r.w4 = twid<DIR>(tw, 4 * base);
+    r.w8 = twid<DIR>(tw, 8 * base);
+    return r;
+}
+__device__ __forceinline__ void apply_tw16(float2* v, const Tw16& p) {
+    const float2 w3 = cmul(p.w2, p.w1);
+    v[1] = cmul(v[1], p.w1);
+    v[2] = cmul(v[2], p.w2);
+    v[3] = cmul(v[3], w3);
+    v[4] = cmul(v[4], p.w4);
+    v[5] = cmul(v[5], cmul(p.w4, p.w1));
+    v[6] = cmul(v[6], cmul(p.w4, p.w2));
+    v[7] = cmul(v[7], cmul(p.w4, w3));
+    v[8] = cmul(v[8], p.w8);
+    v[9] = cmul(v[9], cmul(p.w8, p.w1));
+    v[10] = cmul(v[10], cmul(p.w8, p.w2));
+    v[11] = cmul(v[11], cmul(p.w8, w3));
+    const float2 w12 = cmul(p.w8, p.w4);
+    v[12] = cmul(v[12], w12);
+    v[13] = cmul(v[13], cmul(w12, p.w1));
+    v[14] = cmul(v[14], cmul(w12, p.w2));
+    v[15] = cmul(v[15], cmul(w12, w3));
+}
+
 // One Stockham pass of radix R over NB transforms.  FIRST: input already in
 // registers (time order).  LAST: output left in registers (frequency order).
+// PRE: twiddles of a radix-16 pass supplied by the caller (Q == 1).
 template <int M, int R, int NS, bool FIRST, bool LAST, int DIR, int NB>
 __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
-                                         const float2* __restrict__ tw, int t) {
+                                         const float2* __restrict__ tw, int t,
+                                         const Tw16* pre = nullptr) {
     constexpr int T = M / 16;
     constexpr int Q = 16 / R;
     constexpr int PM = FftShape<M>::PADDED;
@@ -168,7 +205,14 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
             float2 v[R];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = a[nb][q + r * Q];
-            if constexpr (NS > 1) apply_twiddles<R, DIR>(v, tw, k, NS * R);
+            if constexpr (NS > 1) {
+                if constexpr (R == 16) {
+                    if (pre) apply_tw16(v, *pre);
+                    else apply_twiddles<R, DIR>(v, tw, k, NS * R);
+                } else {
+                    apply_twiddles<R, DIR>(v, tw, k, NS * R);
+                }
+            }
             dft<R, DIR>(v);
             if constexpr (LAST) {
 #pragma unroll
@@ -184,12 +228,14 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
 }
 
 // Full transform: radix-16 passes, the leftover factor (2, 4 or 8) last.
-// sm must hold NB * FftShape<M>::PADDED float2.  On return the shared
-// buffer may be reused only after a __syncthreads().
+// t is the thread's index within the group of M/16 threads doing the
+// transform(s); sm must hold NB * FftShape<M>::PADDED float2.  The
+// twiddles of the radix-16 passes after the first are loaded up front.
+// Shared memory may be rewritten as soon as this returns.
 template <int M, int DIR, int NB>
-__device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const float2* __restrict__ tw) {
+__device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const float2* __restrict__ tw,
+                                        int t) {
     static_assert(M >= kMinM && M <= kMaxM && (M & (M - 1)) == 0, "M must be a power of two");
-    const int t = threadIdx.x;
     if constexpr (M == 64) {
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, 4, 16, false, true, DIR, NB>(a, sm, tw, t);
@@ -197,28 +243,27 @@ __device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const f
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, 8, 16, false, true, DIR, NB>(a, sm, tw, t);
     } else if constexpr (M == 256) {
+        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, true, DIR, NB>(a, sm, tw, t);
-    } else if constexpr (M == 512) {
+        fft_pass<M, 16, 16, false, true, DIR, NB>(a, sm, tw, t, &p1);
+    } else if constexpr (M == 512 || M == 1024 || M == 2048) {
+        constexpr int RL = M / 256;
+        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 2, 256, false, true, DIR, NB>(a, sm, tw, t);
-    } else if constexpr (M == 1024) {
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 4, 256, false, true, DIR, NB>(a, sm, tw, t);
-    } else if constexpr (M == 2048) {
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 8, 256, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, RL, 256, false, true, DIR, NB>(a, sm, tw, t);
     } else if constexpr (M == 4096) {
+        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
+        const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 256, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 256, false, true, DIR, NB>(a, sm, tw, t, &p2);
     } else {  // 8192
+        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
+        const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 256, false, false, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 256, false, false, DIR, NB>(a, sm, tw, t, &p2);
         fft_pass<M, 2, 4096, false, true, DIR, NB>(a, sm, tw, t);
     }
 }

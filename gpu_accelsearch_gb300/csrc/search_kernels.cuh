@@ -1,0 +1,534 @@
+// search_kernels.cuh -- the per-step hot path (kernel templates; the
+// instantiations live in search_*.cu).
+//
+//  k_prep   generate_harmonic_ffdot_data + perform_fft_harmonics
+//           (bpd_search.cu:130-184, :228-240): gather the local Fourier
+//           amplitudes, median-normalise the first numdata bins exactly as
+//           the reference does (same float operations, exact lower median),
+//           and FFT.  The reference FFTs the x2 zero-interleaved segment of
+//           L points; its spectrum is the M = L/2 point spectrum of the
+//           un-spread segment repeated twice, so only that is computed.
+//  k_plane  perform_convolution + perform_inversefft + generatePowers
+//           (bpd_search.cu:243-307, bpd_gpu_kernels.cu:39-116) fused: per
+//           template, multiply by the folded template spectrum, two M-point
+//           inverse FFTs in shared memory (even and odd outputs of the
+//           L-point inverse), |y|^2 / L^2 for the valid window, and one
+//           store of the powers.  Nothing but powers reaches global memory.
+//  k_hsum   perform_harmonic_summing / addPowers (bpd_search.cu:310-360,
+//           bpd_gpu_kernels.cu:119-170) with the reference's index
+//           arithmetic, cumulative stage sums in registers, and the
+//           candidate threshold the reference leaves as a stub
+//           (bpd_candidates.cu:4-9), compacted with warp ballots.
+#pragma once
+
+#include "accel_internal.h"
+#include "fft_smem.cuh"
+
+namespace accel {
+
+constexpr double kLn2 = 0.693147180559945309417232121458;
+
+
+// ------------------------------------------------------------------ prep
+template <int M>
+__global__ void __launch_bounds__(M / 16) k_prep(const PrepArgs a, const float2* __restrict__ tw) {
+    constexpr int T = M / 16;
+    constexpr int PM = FftShape<M>::PADDED;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* sm = reinterpret_cast<float2*>(smem_raw);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(sm + PM);
+    __shared__ int hist[256];
+    __shared__ int bc[2];
+    __shared__ float s_norm;
+
+    const HarmPlan& H = a.h[blockIdx.x];
+    const SegDesc sd = a.segs[blockIdx.y];
+    const StepHarm g = step_harm(sd.startr, a.uselen, H.p, H.q, H.hw0);
+    const int t = threadIdx.x;
+    const int numdata = g.numdata < M ? g.numdata : M;  // host checks next_pow2(numdata) == M
+
+    float2 x[1][16];
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        const int idx = t + e * T;
+        const long long b = g.lobin + idx;
+        float2 v = make_float2(0.f, 0.f);
+        if (b >= 0 && b < sd.numbins) v = sd.spec[b];
+        x[0][e] = v;
+        if (idx < numdata) keys[idx] = __float_as_uint(power_exact(v));
+    }
+    __syncthreads();
+    const uint32_t mk = block_select_u32(keys, numdata, (numdata - 1) / 2, hist, bc);
+    if (t == 0) s_norm = rsqrt_magic((float)((double)__uint_as_float(mk) / kLn2));
+    __syncthreads();
+    const float norm = s_norm;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        if (t + e * T < numdata) {
+            x[0][e].x = __fmul_rn(x[0][e].x, norm);
+            x[0][e].y = __fmul_rn(x[0][e].y, norm);
+        }
+    }
+    fft_run<M, -1, 1>(x, sm, tw, t);
+    float2* out = a.dbuf + (long long)blockIdx.y * a.dstride + H.doff;
+#pragma unroll
+    for (int e = 0; e < 16; e++) out[t + e * T] = x[0][e];
+}
+
+// ----------------------------------------------------------------- plane
+// Two layouts of the same work (chosen per context, see accel_set_tuning):
+//   SPLIT = false: M/16 threads, each carries 16 points of both the even and
+//                  the odd transform (shared twiddles, 128 registers);
+//   SPLIT = true:  M/8 threads, the first half does the even transform, the
+//                  second half the odd one (half the registers per thread,
+//                  twice the warps).
+template <bool SPLIT, int M> struct PlaneShape {
+    static constexpr int T = M / 16;
+    static constexpr int THREADS = SPLIT ? M / 8 : M / 16;
+    static constexpr int NB = SPLIT ? 1 : 2;
+    // two CTAs per SM where that leaves 128 registers per thread for the
+    // two-transform layout or 64 for the split one
+    static constexpr int MINB = SPLIT ? (THREADS <= 512 ? 2 : 1) : (THREADS <= 256 ? 2 : 1);
+};
+
+// Multiply the segment spectrum by template z's folded spectrum and run the
+// inverse transform(s).  On return x[nb][e] holds output t + e*T of the even
+// (nb or half 0) / odd (nb or half 1) transform.
+template <int M, bool F16, bool SPLIT>
+__device__ __forceinline__ void plane_transform(const HarmPlan& H, const float2* __restrict__ D, int z,
+                                                float2* sm, const float2* __restrict__ tw,
+                                                float2 (&x)[PlaneShape<SPLIT, M>::NB][16], int t,
+                                                int half) {
+    constexpr int T = M / 16;
+    constexpr int NB = PlaneShape<SPLIT, M>::NB;
+    constexpr int PM = FftShape<M>::PADDED;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        const int idx = t + e * T;
+        const float2 d = D[idx];
+        if constexpr (F16) {
+            const __half2* f = H.fold16 + (size_t)z * 2 * M;
+            const float sc = H.f16scale[z];
+#pragma unroll
+            for (int nb = 0; nb < NB; nb++) {
+                float2 A = __half22float2(f[(SPLIT ? half : nb) * M + idx]);
+                A.x *= sc;
+                A.y *= sc;
+                x[nb][e] = cmul(d, A);
+            }
+        } else {
+            const float2* f = H.fold + (size_t)z * 2 * M;
+#pragma unroll
+            for (int nb = 0; nb < NB; nb++) x[nb][e] = cmul(d, __ldg(f + (SPLIT ? half : nb) * M + idx));
+        }
+    }
+    fft_run<M, +1, NB>(x, sm + (SPLIT ? half * PM : 0), tw, t);
+}
+
+// Stage the row's powers |y|^2 / L^2 for columns [0, wmax) in shared memory
+// (interleaving even and odd outputs) and return the float view.
+template <int M, bool SPLIT>
+__device__ __forceinline__ float* stage_row_powers(const HarmPlan& H, unsigned char* smem_raw,
+                                                   const float2 (&x)[PlaneShape<SPLIT, M>::NB][16],
+                                                   int t, int half) {
+    constexpr int T = M / 16;
+    constexpr int NB = PlaneShape<SPLIT, M>::NB;
+    const float scale = 1.0f / (4.0f * (float)M * (float)M);  // 1 / L^2, exact
+    float* pw = reinterpret_cast<float*>(smem_raw);
+    const int half_w = H.wmax >> 1;
+    __syncthreads();  // every thread has finished reading the transform buffers
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        const int i2 = t + e * T - H.hw0;
+        if (i2 >= 0 && i2 < half_w) {
+#pragma unroll
+            for (int nb = 0; nb < NB; nb++)
+                pw[2 * i2 + (SPLIT ? half : nb)] =
+                    fmaf(x[nb][e].x, x[nb][e].x, x[nb][e].y * x[nb][e].y) * scale;
+        }
+    }
+    __syncthreads();
+    return pw;
+}
+
+template <int M, bool F16, bool SPLIT>
+__global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLIT, M>::MINB)
+    k_plane(const PlaneArgs a, const float2* __restrict__ tw) {
+    constexpr int T = M / 16;
+    constexpr int NB = PlaneShape<SPLIT, M>::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int item = blockIdx.x;
+    int hi = 0;
+#pragma unroll 1
+    while (hi + 1 < a.nh && item >= a.h[hi + 1].zbase) hi++;
+    const HarmPlan& H = a.h[hi];
+    const int z = item - H.zbase;
+    const int seg = blockIdx.y;
+    const int half = SPLIT ? (int)(threadIdx.x / T) : 0;
+    const int t = SPLIT ? (int)(threadIdx.x % T) : (int)threadIdx.x;
+    float2 x[NB][16];
+    plane_transform<M, F16, SPLIT>(H, a.dbuf + (long long)seg * a.dstride + H.doff, z,
+                                   reinterpret_cast<float2*>(smem_raw), tw, x, t, half);
+    // straight from registers: even/odd pairs as 8-byte stores (one thread
+    // holds both), or single floats interleaved by the two halves
+    float* row = a.planes + (long long)seg * a.pstride + H.poff + (long long)z * H.prow;
+    const float scale = 1.0f / (4.0f * (float)M * (float)M);  // 1 / L^2, exact
+    const int half_w = H.wmax >> 1;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        const int i2 = t + e * T - H.hw0;
+        if (i2 >= 0 && i2 < half_w) {
+            if constexpr (NB == 2) {
+                float2 p;
+                p.x = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y) * scale;
+                p.y = fmaf(x[1][e].x, x[1][e].x, x[1][e].y * x[1][e].y) * scale;
+                *reinterpret_cast<float2*>(row + 2 * i2) = p;
+            } else {
+                row[2 * i2 + half] = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y) * scale;
+            }
+        }
+    }
+}
+
+// --------------------------------------------------- fundamental + harmonic sum
+// The fundamental's row z of one segment: transform as in k_plane, then --
+// instead of storing the row -- add the sub-harmonic powers gathered from
+// their planes (computed by earlier k_plane launches of the same group) in
+// the reference's order, check every stage against its cut and append the
+// candidates.  The fundamental plane never reaches global memory.
+__device__ __forceinline__ long long twice_r_shift(long long r2, int p, int lq) {
+    return (2LL * r2 * p + (1LL << lq)) >> (lq + 1);
+}
+__device__ __forceinline__ int trunc_shift(int x, int k) {  // C division by 2^k
+    return x >= 0 ? (x >> k) : -((-x) >> k);
+}
+__device__ __forceinline__ int sub_row(int zz, const HarmPlan& H) {
+    const int d = trunc_shift(zz * H.p, H.lq) - H.zlo;
+    return d >= 0 ? (d >> 1) : -((-d) >> 1);
+}
+
+// Warp-aggregated append of the lanes whose `hit` is set.
+__device__ __forceinline__ void append_candidates(bool hit, int seg, int i, int z, int numharm, float s,
+                                                  RawCand* cands, unsigned long long* ncand,
+                                                  long long cap) {
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(ncand, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (hit) {
+        const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+        if ((long long)slot < cap) {
+            RawCand c;
+            c.seg = seg;
+            c.ridx = i;
+            c.zidx = (int16_t)z;
+            c.numharm = (int16_t)numharm;
+            c.power = s;
+            cands[slot] = c;
+        }
+    }
+}
+
+template <int M, bool F16, bool SPLIT>
+__global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLIT, M>::MINB)
+    k_fund_sum(const FundArgs a, const float2* __restrict__ tw) {
+    constexpr int T = M / 16;
+    constexpr int THREADS = PlaneShape<SPLIT, M>::THREADS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const HarmPlan& H0 = a.h[0];
+    const int z = blockIdx.x;
+    const int seg = blockIdx.y;
+    const int half = SPLIT ? (int)(threadIdx.x / T) : 0;
+    const int t = SPLIT ? (int)(threadIdx.x % T) : (int)threadIdx.x;
+    float2 x[PlaneShape<SPLIT, M>::NB][16];
+    plane_transform<M, F16, SPLIT>(H0, a.dbuf + (long long)seg * a.dstride + H0.doff, z,
+                                   reinterpret_cast<float2*>(smem_raw), tw, x, t, half);
+    const float* pw = stage_row_powers<M, SPLIT>(H0, smem_raw, x, t, half);
+
+    const long long startr = a.segs[seg].startr;
+    const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
+    const int zz = a.zlo0 + kDz * z;
+    int rowoff[kMaxHarm];  // offset of the sub-harmonic row and its rlo*2
+    long long rlo2[kMaxHarm];
+#pragma unroll
+    for (int h = 1; h < kMaxHarm; h++) {
+        if (h < a.nh) {
+            const HarmPlan& H = a.h[h];
+            rowoff[h] = (int)H.poff + sub_row(zz, H) * H.prow;
+            rlo2[h] = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+        }
+    }
+    const int U = a.uselen;
+#pragma unroll 1
+    for (int i0 = 0; i0 < U; i0 += THREADS) {
+        const int i = i0 + threadIdx.x;
+        const bool valid = i < U;
+        float v[kMaxHarm];
+        v[0] = valid ? pw[i] : 0.f;
+#pragma unroll
+        for (int h = 1; h < kMaxHarm; h++) {
+            if (h < a.nh) {
+                const HarmPlan& H = a.h[h];
+                const int rind = (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - rlo2[h]);
+                v[h] = valid ? P[rowoff[h] + rind] : 0.f;
+            }
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int h = 0; h < kMaxHarm; h++) {
+            if (h < a.nh) {
+                s = (h == 0) ? v[0] : s + v[h];
+                const int st = a.stage_of[h];
+                if (st >= 0) {
+                    if (a.stage_out && valid)
+                        a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * U + i] = s;
+                    append_candidates(valid && s > a.cut[st], a.seg_base + seg, i, z, h + 1, s, a.cands,
+                                      a.ncand, a.cap);
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- tiled hsum
+// Harmonic sum of one tile of kTileZ f-dot rows x kTileI columns of the
+// fundamental plane.  The fundamental tile and, for every sub-harmonic, the
+// rectangle of its plane that the tile's (zind, rind) indices touch are
+// copied into shared memory first (16-byte cp.async, each element once per
+// tile), then every cell is summed from shared memory in the reference's
+// harmonic order and checked against the stage cuts.
+constexpr int kTileZ = kHsumTileZ;
+constexpr int kTileI = kHsumTileI;
+constexpr int kTileSmemFloats = kHsumTileFloats;   // 60 KB: fundamental tile + sub-tiles
+
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Stage index after harmonic h (bank order): stages end after 1, 2, 4, 8,
+// 16 harmonics (bpd_search.cu:350), i.e. when h + 1 is a power of two.
+__host__ __device__ constexpr int stage_after(int h) {
+    return ((h + 1) & h) ? -1 : (h == 0 ? 0 : h == 1 ? 1 : h == 3 ? 2 : h == 7 ? 3 : 4);
+}
+
+template <int NH, bool STAGE_OUT>
+__global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
+    extern __shared__ __align__(16) float tsm[];
+    __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
+    const int seg = blockIdx.z;
+    const int z0 = blockIdx.y * kTileZ;
+    const int i0 = blockIdx.x * kTileI;
+    const int nz = min(kTileZ, a.numzs0 - z0);
+    const int ni = min(kTileI, a.uselen - i0);
+    const long long startr = a.segs[seg].startr;
+    const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
+    const int tid = threadIdx.x;
+    const int i = i0 + tid;
+    const bool valid = tid < ni;
+
+    // Rectangles: rows [zf, zl] and 4-aligned columns [c0, c0 + 4*w4) per harmonic.
+    int col[NH];
+    int off = 0;
+#pragma unroll
+    for (int h = 0; h < NH; h++) {
+        const HarmPlan& H = a.h[h];
+        int rfirst, rlast, zf, zl, mycol;
+        if (h == 0) {
+            rfirst = i0;
+            rlast = i0 + ni - 1;
+            zf = z0;
+            zl = z0 + nz - 1;
+            mycol = i;
+        } else {
+            const long long rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+            rfirst = (int)(unsigned short)(twice_r_shift(2 * startr + i0, H.p, H.lq) - rlo2);
+            rlast = (int)(unsigned short)(twice_r_shift(2 * startr + i0 + ni - 1, H.p, H.lq) - rlo2);
+            mycol = valid ? (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - rlo2) : rfirst;
+            zf = sub_row(a.zlo0 + kDz * z0, H);
+            zl = sub_row(a.zlo0 + kDz * (z0 + nz - 1), H);
+        }
+        const int c0 = rfirst & ~3;
+        const int w4 = ((rlast - c0) >> 2) + 1;  // 16-byte chunks per row
+        col[h] = off + (mycol - c0);
+        if (tid < nz) {
+            const int zr = tid;
+            const int r = (h == 0) ? zr : sub_row(a.zlo0 + kDz * (z0 + zr), H) - zf;
+            s_row[h][zr] = 4 * w4 * r;
+        }
+        const int nzr = zl - zf + 1;
+        const float* src = P + H.poff + (long long)zf * H.prow + c0;
+        for (int r = tid >> 5; r < nzr; r += kTileI / 32)
+            for (int c = tid & 31; c < w4; c += 32)
+                cp_async16(tsm + off + 4 * (r * w4 + c), src + (long long)r * H.prow + 4 * c);
+        off += 4 * nzr * w4;
+    }
+    float cut[kMaxStages];
+#pragma unroll
+    for (int st = 0; st < kMaxStages; st++) cut[st] = a.cut[st];
+    cp_async_wait_all();
+    __syncthreads();
+
+#pragma unroll 2
+    for (int zr = 0; zr < nz; zr++) {
+        const int z = z0 + zr;
+        float s = 0.f;
+#pragma unroll
+        for (int h = 0; h < NH; h++) {
+            const float v = tsm[s_row[h][zr] + col[h]];
+            s = (h == 0) ? v : s + v;
+            const int st = stage_after(h);  // folds to a constant once h is unrolled
+            if (st >= 0) {
+                if constexpr (STAGE_OUT) {
+                    if (valid)
+                        a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
+                }
+                append_candidates(valid && s > cut[st], a.seg_base + seg, i, z, h + 1, s, a.cands,
+                                  a.ncand, a.cap);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ hsum
+// One thread per fundamental column i, kHsumRows f-dot rows per block.  The
+// reference's index arithmetic (twice_required_r, sub_zind) divides by
+// powers of two only, so it is done with shifts here; the per-column
+// sub-harmonic offsets are computed once per thread.
+constexpr int kHsumCols = 128;
+constexpr int kHsumRows = 32;
+
+template <int NH>
+__global__ void __launch_bounds__(kHsumCols) k_hsum(const HsumArgs a) {
+    const int i = blockIdx.x * kHsumCols + threadIdx.x;
+    const int seg = blockIdx.z;
+    const bool valid = i < a.uselen;
+    const long long startr = a.segs[seg].startr;
+    const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
+    const int lane = threadIdx.x & 31;
+
+    int roff[NH];
+#pragma unroll
+    for (int h = 1; h < NH; h++) {
+        const HarmPlan& H = a.h[h];
+        const long long rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+        const int rind = (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - rlo2);
+        roff[h] = (int)H.poff + rind;
+    }
+    const int z0 = blockIdx.y * kHsumRows;
+    const int zend = min(z0 + kHsumRows, a.numzs0);
+    const int base0 = (int)a.h[0].poff + i;
+#pragma unroll 2
+    for (int z = z0; z < zend; z++) {
+        const int zz = a.zlo0 + kDz * z;
+        float v[NH];
+        v[0] = valid ? P[base0 + z * a.h[0].prow] : 0.f;
+#pragma unroll
+        for (int h = 1; h < NH; h++) {
+            const HarmPlan& H = a.h[h];
+            const int d = trunc_shift(zz * H.p, H.lq) - H.zlo;
+            const int zind = d >= 0 ? (d >> 1) : -((-d) >> 1);
+            v[h] = valid ? P[roff[h] + zind * H.prow] : 0.f;
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int h = 0; h < NH; h++) {
+            s = (h == 0) ? v[0] : s + v[h];
+            const int st = stage_after(h);  // folds to a constant once h is unrolled
+            if (st >= 0) {
+                if (a.stage_out && valid)
+                    a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
+                const bool hit = valid && s > a.cut[st];
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (m) {
+                    unsigned long long base = 0;
+                    const int leader = __ffs(m) - 1;
+                    if (lane == leader) base = atomicAdd(a.ncand, (unsigned long long)__popc(m));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    if (hit) {
+                        const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+                        if ((long long)slot < a.cap) {
+                            RawCand c;
+                            c.seg = a.seg_base + seg;
+                            c.ridx = i;
+                            c.zidx = (int16_t)z;
+                            c.numharm = (int16_t)(h + 1);
+                            c.power = s;
+                            a.cands[slot] = c;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------- launchers
+template <int M> static int prep_m(const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    size_t smem = sizeof(float2) * FftShape<M>::PADDED + sizeof(uint32_t) * M;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    k_prep<M><<<dim3(a.nh, nseg), M / 16, smem, st>>>(a, tw);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int M, bool F16, bool SPLIT>
+static int plane_m(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    size_t smem = sizeof(float2) * FftShape<M>::PADDED * 2;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    k_plane<M, F16, SPLIT><<<dim3(a.ntpl, nseg), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int M>
+static int plane_dispatch(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    const bool h = a.use_fp16 != 0, sp = a.split != 0;
+    if (h) return sp ? plane_m<M, true, true>(a, nseg, tw, st) : plane_m<M, true, false>(a, nseg, tw, st);
+    return sp ? plane_m<M, false, true>(a, nseg, tw, st) : plane_m<M, false, false>(a, nseg, tw, st);
+}
+
+template <int M, bool F16, bool SPLIT>
+static int fund_m(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    size_t smem = sizeof(float2) * FftShape<M>::PADDED * 2;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_fund_sum<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_fund_sum<M, F16, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    k_fund_sum<M, F16, SPLIT><<<dim3(a.h[0].numzs, nseg), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int M>
+static int fund_dispatch(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    const bool h = a.use_fp16 != 0, sp = a.split != 0;
+    if (h) return sp ? fund_m<M, true, true>(a, nseg, tw, st) : fund_m<M, true, false>(a, nseg, tw, st);
+    return sp ? fund_m<M, false, true>(a, nseg, tw, st) : fund_m<M, false, false>(a, nseg, tw, st);
+}
+
+}  // namespace accel

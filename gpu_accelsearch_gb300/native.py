@@ -42,13 +42,19 @@ class Candidate(C.Structure):
                 ("numharm", C.c_int), ("power", C.c_float), ("sigma", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("chunk_segments", C.c_int), ("plane_split", C.c_int), ("fused_sum", C.c_int),
+                ("hsum_rowwise", C.c_int), ("serial_sum", C.c_int),
+                ("reserved", C.c_int * 3)]
+
+
 class Stats(C.Structure):
-    _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 5),
-                ("kind_ms", C.c_double * 5), ("segments", C.c_longlong),
-                ("cells", C.c_longlong)]
+    _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 6),
+                ("kind_ms", C.c_double * 6), ("segments", C.c_longlong),
+                ("cells", C.c_longlong), ("search_ms", C.c_double), ("searches", C.c_longlong)]
 
 
-KINDS = ["prep", "plane", "hsum", "whiten", "rfft"]
+KINDS = ["prep", "plane", "hsum", "whiten", "rfft", "fund"]
 
 _vp, _ll, _llp = C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)
 SIGNATURES = {
@@ -62,6 +68,8 @@ SIGNATURES = {
     "accel_profile": (C.c_int, [_vp, C.c_int]),
     "accel_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "accel_reset_stats": (C.c_int, [_vp]),
+    "accel_get_tuning": (C.c_int, [_vp, C.POINTER(Tuning)]),
+    "accel_set_tuning": (C.c_int, [_vp, C.POINTER(Tuning)]),
     "accel_num_harmonics": (C.c_int, [_vp]),
     "accel_num_stages": (C.c_int, [_vp]),
     "accel_uselen": (C.c_int, [_vp]),
@@ -74,6 +82,8 @@ SIGNATURES = {
     "accel_harmonic_indices": (C.c_int, [_ll, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
+    "accel_autotune": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                 C.POINTER(Config), C.POINTER(Tuning), C.POINTER(C.c_double)]),
     "accel_search": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), _llp, C.POINTER(C.c_double),
                                C.c_int, _llp]),
     "accel_search_spectra": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), _llp, _llp, _llp]),

@@ -52,6 +52,24 @@ def first_bin(nsamples: int, dt: float) -> int:
     return N.lib().accel_first_bin(nsamples, dt)
 
 
+def autotune(zmax=200, numharm=8, fftlens=(4096, 8192, 16384), steps=64, template_fp16=False,
+             device=0):
+    """Pick the segment length and launch shape by timing them on this GPU.
+    Returns (kwargs for AccelSearch, tuning dict, cells/s)."""
+    L = N.lib()
+    base = N.Config()
+    L.accel_config_init(C.byref(base))
+    base.zmax, base.numharm, base.template_fp16, base.device = zmax, numharm, int(template_fp16), device
+    fl = (C.c_int * len(fftlens))(*fftlens)
+    best, tun, rate = N.Config(), N.Tuning(), C.c_double()
+    N.check(L.accel_autotune(C.byref(base), fl, len(fftlens), steps, C.byref(best), C.byref(tun),
+                             C.byref(rate)))
+    kw = dict(zmax=zmax, numharm=numharm, fftlen=best.fftlen, template_fp16=template_fp16,
+              chunk_segments=best.chunk_segments, device=device)
+    return kw, {"chunk_segments": tun.chunk_segments, "plane_split": tun.plane_split,
+                "fused_sum": tun.fused_sum}, rate.value
+
+
 class AccelSearch:
     def __init__(self, zmax=200, numharm=8, fftlen=8192, uselen=0, sigma=6.0, numindep=1.0,
                  whiten_initbuf=6, whiten_maxbuf=200, template_fp16=False, chunk_segments=0,
@@ -65,6 +83,8 @@ class AccelSearch:
         cfg.template_fp16 = int(bool(template_fp16))
         cfg.chunk_segments, cfg.cand_capacity, cfg.device = chunk_segments, cand_capacity, device
         self.config = cfg
+        self.kwargs = dict(zmax=zmax, numharm=numharm, fftlen=fftlen, template_fp16=template_fp16,
+                           chunk_segments=chunk_segments, device=device)
         h = C.c_void_p()
         N.check(L.accel_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -123,6 +143,24 @@ class AccelSearch:
         N.check(N.lib().accel_bank_spectra(self._h, h, k.ctypes.data, f.ctypes.data))
         return k, f
 
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(N.lib().accel_get_tuning(self._h, C.byref(t)))
+        return {"chunk_segments": t.chunk_segments, "plane_split": t.plane_split,
+                "fused_sum": t.fused_sum,
+                "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum}
+
+    def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
+                   hsum_rowwise=None, serial_sum=None):
+        cur = self.tuning()
+        t = N.Tuning()
+        t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
+        t.plane_split = cur["plane_split"] if plane_split is None else int(plane_split)
+        t.fused_sum = cur["fused_sum"] if fused_sum is None else int(fused_sum)
+        t.hsum_rowwise = cur["hsum_rowwise"] if hsum_rowwise is None else int(hsum_rowwise)
+        t.serial_sum = cur["serial_sum"] if serial_sum is None else int(serial_sum)
+        N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
+
     def profile(self, enable: bool = True):
         N.check(N.lib().accel_profile(self._h, int(enable)))
 
@@ -130,6 +168,7 @@ class AccelSearch:
         st = N.Stats()
         N.check(N.lib().accel_get_stats(self._h, C.byref(st)))
         return {"launches": st.launches, "segments": st.segments, "cells": st.cells,
+                "search_ms": st.search_ms, "searches": st.searches,
                 "kinds": {k: {"launches": st.kind_launches[i], "ms": st.kind_ms[i]}
                           for i, k in enumerate(N.KINDS)}}
 

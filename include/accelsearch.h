@@ -72,16 +72,34 @@ typedef struct accel_candidate {
 } accel_candidate;
 
 /* Kernel accounting of a context (accel_get_stats).  Kinds: 0 segment
- * preparation, 1 power planes, 2 harmonic sum, 3 whitening, 4 R2C FFT
- * (cuFFT; not counted in `launches`). */
-#define ACCEL_KINDS 5
+ * preparation, 1 power planes, 2 harmonic sum (stage API), 3 whitening,
+ * 4 R2C FFT (cuFFT; not counted in `launches`), 5 fundamental plane fused
+ * with the harmonic sum (search path). */
+#define ACCEL_KINDS 6
 typedef struct accel_stats {
     long long launches;                 /* kernels of this library launched   */
     long long kind_launches[ACCEL_KINDS];
     double kind_ms[ACCEL_KINDS];        /* CUDA-event time when profiling      */
     long long segments;                 /* overlap-save steps searched         */
     long long cells;                    /* fundamental f-fdot cells searched   */
+    double search_ms;                   /* CUDA-event time of the accel_search* */
+                                        /* calls, first copy to last read-back */
+    long long searches;
 } accel_stats;
+
+/* Launch shape of a context's search (accel_get_tuning/accel_set_tuning). */
+typedef struct accel_tuning {
+    int chunk_segments;     /* overlap-save steps per launch group            */
+    int plane_split;        /* plane kernel: 0 one thread carries the even and */
+                            /* the odd transform, 1 separate threads          */
+    int fused_sum;          /* 1: sum harmonics inside the fundamental's plane */
+                            /* kernel; 0: store all planes, tiled sum kernel  */
+    int hsum_rowwise;       /* 1: row-wise harmonic-sum kernel instead of the  */
+                            /* shared-memory tiled one                        */
+    int serial_sum;         /* 1: no overlap of a group's harmonic sum (second */
+                            /* stream) with the next group's transforms       */
+    int reserved[3];
+} accel_tuning;
 
 typedef struct accel_ctx accel_ctx;
 
@@ -98,6 +116,10 @@ int  accel_synchronize(accel_ctx *ctx);
 int  accel_profile(accel_ctx *ctx, int enable);
 int  accel_get_stats(accel_ctx *ctx, accel_stats *out);
 int  accel_reset_stats(accel_ctx *ctx);
+
+int  accel_get_tuning(const accel_ctx *ctx, accel_tuning *out);
+/* Changing chunk_segments reallocates the per-group work buffers. */
+int  accel_set_tuning(accel_ctx *ctx, const accel_tuning *t);
 
 int  accel_num_harmonics(const accel_ctx *ctx);
 int  accel_num_stages(const accel_ctx *ctx);
@@ -123,6 +145,14 @@ int  accel_step_harmonic(long long startr, int uselen, int harmnum, int maxharm,
  * sub-harmonic zlo_h). */
 int  accel_harmonic_indices(long long startr, int uselen, int harmnum, int maxharm, int hw0,
                             int zlo0, int zlo_h, int nr, int nz, int *rind, int *zind);
+
+/* Autotuner: for each segment length fftlens[i] (others from *base) build a
+ * context, whiten a seeded synthetic spectrum on the device and time a
+ * search of `steps` overlap-save steps for every launch shape; the fastest
+ * (fundamental f-fdot cells per second) is returned in best_cfg (with its
+ * chunk_segments) and best_tuning, its rate in *best_rate. */
+int  accel_autotune(const accel_config *base, const int *fftlens, int nlens, int steps,
+                    accel_config *best_cfg, accel_tuning *best_tuning, double *best_rate);
 
 /* ------------------------------------------------------------ whole search */
 /* Search ntrials time series: R2C FFT, whitening, every overlap-save step,

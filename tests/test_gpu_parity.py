@@ -216,3 +216,49 @@ def test_batched_equals_single(S, trial):
     both = np.concatenate([c1, c2b])
     assert np.array_equal(np.sort(cb, order=["trial", "step", "numharm", "z", "r"]),
                           np.sort(both, order=["trial", "step", "numharm", "z", "r"]))
+
+
+@pytest.mark.parametrize("split,fused,chunk,serial,rowwise",
+                         [(0, 1, 7, 0, 0), (1, 1, 64, 1, 0), (0, 0, 64, 1, 0), (1, 0, 1, 0, 0),
+                          (0, 0, 33, 0, 1), (1, 0, 5, 0, 0), (0, 0, 2, 0, 0)])
+def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwise):
+    # every launch shape gives bit-identical candidates (same float operations)
+    w, rlo = trial["w"], trial["rlo"]
+    d = dev(w)
+    S.set_power_cuts(np.array([6.6, 9.2, 13.1], np.float32))  # ~3 sigma: many candidates
+    try:
+        S.set_tuning(chunk_segments=64, plane_split=0, fused_sum=0, serial_sum=1,
+                     hsum_rowwise=0)
+        S.search_spectra([d.data_ptr()], [w.size], [rlo])
+        base = S.candidates()
+        S.set_tuning(chunk_segments=chunk, plane_split=split, fused_sum=fused,
+                     serial_sum=serial, hsum_rowwise=rowwise)
+        S.search_spectra([d.data_ptr()], [w.size], [rlo])
+        got = S.candidates()
+    finally:
+        S.set_tuning(chunk_segments=64, plane_split=0, fused_sum=0, serial_sum=1,
+                     hsum_rowwise=0)
+        S.set_power_cuts([O.power_cut(6.0, 1 << s) for s in range(S.nstages)])
+    assert len(base) > 10000
+    assert np.array_equal(base, got)
+
+
+def test_many_candidates_match_oracle(S, trial, orc):
+    # ~3 sigma cuts: tens of thousands of candidates through the compaction
+    w, rlo = trial["w"], trial["rlo"]
+    d = dev(w)
+    cuts = np.array([6.6, 9.2, 13.1], np.float32)
+    S.set_power_cuts(cuts)
+    try:
+        S.search_spectra([d.data_ptr()], [w.size], [rlo])
+        gpu = S.candidates()
+    finally:
+        S.set_power_cuts([O.power_cut(6.0, 1 << s) for s in range(S.nstages)])
+    steps = 12
+    gpu = gpu[gpu["step"] < steps]
+    c64 = cuts.astype(np.float64)
+    o_lo, _, _ = orc.run_steps(w, rlo, 0, steps, powcut=c64 * (1 - TOL_P), cap=1 << 22)
+    o_hi, _, _ = orc.run_steps(w, rlo, 0, steps, powcut=c64 * (1 + TOL_P), cap=1 << 22)
+    g = _keyset(gpu, rlo, S.uselen // 2, -50)
+    assert len(g) > 2000
+    assert _keyset(o_hi, 0, 0, 0) <= g <= _keyset(o_lo, 0, 0, 0)
