@@ -96,6 +96,9 @@ struct WhitenPlanDev {
     double* d_med = nullptr;
 };
 
+}  // namespace
+
+namespace accel {
 // Serial block recurrence of deredden (bpd_noise.c:33-79).
 std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbuf, int maxbuf) {
     std::vector<std::pair<int, int>> b;
@@ -112,6 +115,9 @@ std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbu
     }
     return b;
 }
+}  // namespace accel
+
+namespace {
 
 struct TrialBuf {
     long long n = 0;
@@ -942,6 +948,14 @@ int accel_set_power_cuts(accel_ctx* c, const float* cuts) {
     if (!c || !cuts) return set_err(ACCEL_ERR_INVALID, "null argument");
     for (int s = 0; s < c->nstages; s++) c->cuts[s] = cuts[s];
     return ACCEL_OK;
+}
+
+double accel_power_cut(double sigma, int numharm, double numindep) {
+    return power_cut(sigma, numharm, numindep);
+}
+
+double accel_sigma_of_power(double power, int numharm, double numindep) {
+    return sigma_of_power(power, numharm, numindep);
 }
 
 long long accel_first_bin(long long nsamples, double dt) {

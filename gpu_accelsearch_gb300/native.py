@@ -77,6 +77,8 @@ SIGNATURES = {
     "accel_get_power_cuts": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "accel_set_power_cuts": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "accel_first_bin": (_ll, [_ll, C.c_double]),
+    "accel_power_cut": (C.c_double, [C.c_double, C.c_int, C.c_double]),
+    "accel_sigma_of_power": (C.c_double, [C.c_double, C.c_int, C.c_double]),
     "accel_step_count": (_ll, [_vp, _ll, C.c_double]),
     "accel_step_harmonic": (C.c_int, [_ll, C.c_int, C.c_int, C.c_int, C.c_int, _llp]),
     "accel_harmonic_indices": (C.c_int, [_ll, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -132,6 +132,11 @@ int  accel_set_power_cuts(accel_ctx *ctx, const float *cuts);
  * first bin rlo = floor(n*dt) (AccelSearch.cu:101) and the number of
  * overlap-save steps (AccelSearch.cu:209). */
 long long accel_first_bin(long long nsamples, double dt);
+/* Power of an n-harmonic sum whose Gamma(n,1) tail equals the one-sided
+ * Gaussian tail at sigma divided by numindep (the stage cut), and the
+ * inverse (a candidate's significance). */
+double accel_power_cut(double sigma, int numharm, double numindep);
+double accel_sigma_of_power(double power, int numharm, double numindep);
 long long accel_step_count(const accel_ctx *ctx, long long nsamples, double dt);
 /* Geometry of one harmonic (harmnum/maxharm, widest halfwidth hw0) for the
  * step starting at startr (generate_harmonics_ffdot, bpd_search.cu:72-127,

@@ -1,0 +1,141 @@
+/*
+ * bpd_compat.h -- the reference pipeline API of keithasr/gpu_accelsearch,
+ * same function names, structs and argument meaning, implemented by
+ * libaccelsearch.so on its own GB300 kernels.  A caller of the reference's
+ * headers/bpd_search.cuh, bpd_subharmonics.cuh, bpd_fft.cuh, bpd_noise.h and
+ * bpd_candidates.cuh includes this header instead and links
+ * -laccelsearch.  Everything here has C linkage (the reference's .cu
+ * functions have C++ linkage; a C++ caller includes this header and gets the
+ * same names).
+ *
+ * Differences kept on purpose: errors do not exit the process -- the
+ * functions are void as in the reference, so check accel_compat_status()
+ * (0 or a negative ACCEL_ERR_*, message in accel_last_error()); and the
+ * reference's compile-time ACCEL_USELEN (32000) is a runtime setting
+ * (accel_compat_set_uselen).  Device pointers are ordinary cudaMalloc
+ * memory, as in the reference; the work runs on the legacy default stream.
+ */
+#ifndef BPD_COMPAT_H_
+#define BPD_COMPAT_H_
+
+#include "accelsearch.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* headers/bpd_subharmonics.cuh:13-25 */
+typedef struct SubharmonicInfo {
+    unsigned short maxHarmonic;
+    unsigned short currentHarmonic;
+    int zmax;
+    unsigned short totalKernelsTemplates;
+    int kernelFFTLength;
+    int *z;
+    unsigned short *kernelHalfWidth;
+    accel_complex *kernels_data;        /* device: FFT of the wrapped templates */
+} SubharmonicInfo;
+
+/* headers/bpd_search.cuh:15-32 */
+typedef struct ffdotInfo {
+    unsigned short currentHarmonic;
+    unsigned short maxHarmonic;
+    int numrs;
+    int numzs;
+    int rlo;
+    int zlo;
+    double rhi;
+    int fftlen;
+} ffdotInfo;
+
+/* headers/bpd_candidates.cuh:15-36 */
+typedef struct RDERIVS {
+    double pow, phs, dpow, dphs, d2pow, d2phs, locpow;
+} rderivs;
+
+typedef struct Candidates {
+    float power;
+    float sigma;
+    int numharm;
+    double r;
+    double z;
+    double *pows;
+    double *hirs;
+    double *hizs;
+    rderivs *derivs;
+} Candidates;
+
+/* Runtime replacement of the reference's ACCEL_USELEN (bpd_common.h:24),
+ * default 32000; it must be even and below 65536. */
+void accel_compat_set_uselen(int uselen);
+int  accel_compat_get_uselen(void);
+/* Status of the last drop-in call (ACCEL_OK or ACCEL_ERR_*). */
+int  accel_compat_status(void);
+
+/* bpd_subharmonics.cuh:27-33 */
+SubharmonicInfo *createSubharmonicInfo(int numHarmonicStages, int zhi);
+int    calc_required_z(double harmonicFraction, double zfull);
+double calc_required_r(double harmonicFraction, double rfull);
+int    index_from_r(double r, double rlo);
+int    index_from_z(double z, double zlo);
+int    getTotalHarmonics(int harmonicStages);
+/* Frees what createSubharmonicInfo allocated (the reference's caller does
+ * this by hand, AccelSearch.cu:272-277). */
+void   freeSubharmonicInfo(SubharmonicInfo *shi, int totalHarmonics);
+
+/* bpd_fft.cuh:14-16: realToComplexFFT takes host samples and returns a
+ * malloc'd host spectrum of n/2+1 bins (caller frees), like the reference. */
+unsigned realToComplexFFT(float *idata, long inputElements, accel_complex **odata, int batch);
+unsigned complexToComplexFFT(accel_complex *device_idata, unsigned int inputElements,
+                             accel_complex **device_odata, int batch);
+unsigned inverseComplexToComplexFFT(accel_complex *device_idata, unsigned int inputElements,
+                                    accel_complex **device_odata, int batch);
+
+/* bpd_noise.h:16 -- host spectrum, whitened on the GPU, in place. */
+void deredden(accel_complex *fft, unsigned numOfBins);
+
+/* bpd_search.cuh:37-46 */
+void generate_harmonics_ffdot(unsigned short totalHarmonics, unsigned short harmonicStages,
+                              SubharmonicInfo *subharmonicsInfo, double fullrlo, double fullrhi,
+                              double zlo, ffdotInfo *output_ffdot,
+                              unsigned short *output_binOffsetArray);
+void generate_harmonic_ffdot_data(unsigned short totalHarmonics, long totalDataLength,
+                                  ffdotInfo *ffdot, unsigned short *binoffsetArray,
+                                  long *dataStartIdx, accel_complex *fft, long dataNumbins,
+                                  long dataLoBin, accel_complex *output_data);
+void perform_fft_harmonics(unsigned short totalHarmonics, accel_complex *device_data,
+                           long *dataStartIdx, accel_complex *output_device_fftdata);
+void perform_convolution(unsigned short totalHarmonics, accel_complex *device_fft_data,
+                         ffdotInfo *harmonicInfo, SubharmonicInfo *shi, long *dataStartIdx,
+                         accel_complex *output_deviceConvolvedSignal,
+                         long *convolutionHarmonicIdx);
+void perform_inversefft(unsigned short totalHarmonics, accel_complex *device_convolvedSignal,
+                        long *convolutionHarmonicIdx, accel_complex *output_device_ifftdata);
+void generate_fundamental_powers(unsigned short totalHarmonics, accel_complex *device_ifft_data,
+                                 long *ifftHarmonicIdx, ffdotInfo *harmonicInfo,
+                                 SubharmonicInfo *shi, float *output_devicePowers);
+void perform_harmonic_summing(unsigned short totalHarmonics, accel_complex *device_ifft_data,
+                              long *ifftHarmonicIdx, ffdotInfo *harmonicInfo,
+                              SubharmonicInfo *shi, float *output_devicePowers, int fullrlo,
+                              unsigned short *host_rinds, unsigned short *device_rinds,
+                              int totalRindsBins);
+void initialize_cuda_plans(unsigned short totalHarmonics, SubharmonicInfo *subharmonicInfo);
+void free_cuda_plans(unsigned short totalHarmonics);
+
+/* bpd_candidates.cuh:40 (a stub in the reference).  Here: the cells of the
+ * power plane left by the last perform_harmonic_summing (or, before any
+ * summing, generate_fundamental_powers) whose power exceeds powcut, as a
+ * malloc'd array (caller frees) of at most *ncand entries in, the number
+ * found out.  ffdot is the step's harmonic info (ffdot[0] the fundamental),
+ * numharm the harmonics summed in that plane; sigma uses numindep. */
+Candidates *search_ffdot_powers_n(ffdotInfo *ffdot, int numharm, float powcut,
+                                  long long numindep, long *ncand);
+/* The reference's signature: same as above, returning the array; the
+ * `cands` argument is ignored (the reference returns it unchanged). */
+Candidates *search_ffdot_powers(ffdotInfo *ffdot, int numharm, float powcut, long long numindep,
+                                Candidates *cands);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BPD_COMPAT_H_ */
