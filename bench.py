@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--serving-seconds", type=float, default=5.0,
+                    help="duration of the Poisson arrival process of the serving leg (0: skip)")
     return ap.parse_args()
 
 
@@ -137,6 +139,76 @@ def device_series(torch, lengths, sigs, seed):
             x += (amp * torch.cos(2 * np.pi * (r0 * t + 0.5 * z * t * t))).float()
         out.append(x)
     return out
+
+
+# ----------------------------------------------------------------- serving
+def smooth_length(n: int) -> int:
+    """Smallest even 7-smooth length >= n (observations are padded to
+    FFT-friendly lengths)."""
+    m = n + (n & 1)
+    while True:
+        k = m
+        for p in (2, 3, 5, 7):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m += 2
+
+def run_serving(seconds: float, device: int, rate: float = 200.0):
+    """The serving configuration: Poisson arrivals at `rate` per second of
+    DM-trial series with lengths log-uniform in 2^18..2^23 samples, zmax
+    uniform in {50, 100, 200, 300}, 5% with an injected signal, admitted
+    against a 150 GB HBM budget.  Requests are slices of a pool of seeded
+    host series (the server reads a request's samples when it admits it)."""
+    from gpu_accelsearch_gb300.serving import Server
+    from gpu_accelsearch_gb300.synth import synth_series
+    rng = np.random.default_rng(4242)
+    nmax = 1 << 23
+    pool = [synth_series(nmax, seed=700 + i) for i in range(8)]
+    sig = [synth_series(nmax, seed=800 + i, signals=[(0.05, 1e5 * (i + 1), 20.0 * (i - 2))])
+           for i in range(4)]
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        n = smooth_length(int(2 ** rng.uniform(18, 23)))
+        zmax = int(rng.choice([50, 100, 200, 300]))
+        src = sig[rng.integers(len(sig))] if rng.random() < 0.05 else pool[rng.integers(len(pool))]
+        arrivals.append((t, src[:n], zmax))
+    srv = Server(hbm_budget_bytes=150e9, fftlen=8192, numharm=8, chunk_segments=128, device=device)
+    for z in (50, 100, 200, 300):  # build the four banks outside the measurement
+        srv.wait(srv.submit(pool[0][: 1 << 18], DT, z), -1)
+    base = srv.stats()
+    t0 = time.perf_counter()
+    ids = []
+    for ta, x, z in arrivals:
+        dly = t0 + ta - time.perf_counter()
+        if dly > 0:
+            time.sleep(dly)
+        ids.append(srv.submit(x, DT, z))
+    lats = []
+    for rid in ids:
+        srv.wait(rid, -1)
+        lats.append(srv.result(rid)[1])
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    cells = st["cells"] - base["cells"]
+    gpu_s = (st["gpu_ms"] - base["gpu_ms"]) / 1e3
+    lats = np.array(lats)
+    return {"requests": len(ids), "offered_rate_per_s": rate, "arrival_seconds": seconds,
+            "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
+            "mean_ms": float(lats.mean()), "max_ms": float(lats.max()),
+            "cells_per_s": cells / wall, "cells_per_gpu_s": cells / gpu_s if gpu_s else None,
+            "worker_admit_s": (st["admit_ms"] - base["admit_ms"]) / 1e3,
+            "worker_group_s": (st["group_ms"] - base["group_ms"]) / 1e3,
+            "wall_s": wall, "hbm_budget_bytes": 150e9,
+            "workload": "Poisson arrivals, lengths log-uniform 2^18..2^23 (rounded up to even "
+                        "7-smooth lengths), "
+                        "zmax uniform in {50,100,200,300}, 5% with a signal, L=8192, 8 harmonics, "
+                        "continuous batching (accel_server)"}
 
 
 # ------------------------------------------------------------ cpu baseline
@@ -375,6 +447,7 @@ def run_ours(args):
     kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
     cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
@@ -396,6 +469,7 @@ def run_ours(args):
         "plain": plain,
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "candidates_per_step": ncand,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     s.close()

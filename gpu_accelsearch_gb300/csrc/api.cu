@@ -20,6 +20,7 @@
 
 #include "../../include/accelsearch.h"
 #include "accel_internal.h"
+#include "context.h"
 
 using namespace accel;
 
@@ -77,25 +78,23 @@ double power_cut(double sigma, int numharm, double numindep) {
     }
     return 0.5 * (lo + hi);
 }
+// Equivalent Gaussian significance: solve log Q(sigma) = logp with Newton
+// steps on log Q, whose derivative is -phi(s)/Q(s) (the inverse Mills ratio).
 double sigma_of_power(double power, int numharm, double numindep) {
-    double logp = log_gamma_q(numharm, power) + std::log(numindep > 1.0 ? numindep : 1.0);
+    const double logp = log_gamma_q(numharm, power) + std::log(numindep > 1.0 ? numindep : 1.0);
     if (logp >= std::log(0.5)) return 0.0;
-    double lo = 0.0, hi = 200.0;
-    for (int it = 0; it < 200; it++) {
-        double mid = 0.5 * (lo + hi);
-        if (log_gauss_tail(mid) > logp) lo = mid;
-        else hi = mid;
+    double s = std::sqrt(-2.0 * logp);  // asymptotic start, slightly above the root
+    for (int it = 0; it < 50; it++) {
+        const double f = log_gauss_tail(s) - logp;
+        const double lphi = -0.5 * s * s - 0.5 * std::log(2.0 * M_PI);
+        const double d = -std::exp(lphi - log_gauss_tail(s));  // d/ds log Q(s)
+        const double step = f / d;
+        s -= step;
+        if (s < 0.0) s = 0.0;
+        if (std::fabs(step) < 1e-10 * (1.0 + s)) break;
     }
-    return 0.5 * (lo + hi);
+    return s;
 }
-
-struct WhitenPlanDev {
-    int nb = 0, maxlen = 0;
-    int* d_start = nullptr;
-    int* d_len = nullptr;
-    double* d_med = nullptr;
-};
-
 }  // namespace
 
 namespace accel {
@@ -117,75 +116,8 @@ std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbu
 }
 }  // namespace accel
 
-namespace {
 
-struct TrialBuf {
-    long long n = 0;
-    float* series = nullptr;
-    float2* spec = nullptr;
-};
-
-}  // namespace
-
-struct accel_ctx {
-    accel_config cfg{};
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int uselen = 0, nh = 0, nstages = 0, numzs0 = 0, zlo0 = 0;
-
-    // bank
-    BankHarmDev bh[kMaxHarm]{};
-    BankHarmDev* d_bh = nullptr;
-    void* bank_mem = nullptr;
-    int ntpl = 0;
-    float2* tw = nullptr;
-
-    // plan
-    HarmPlan hp[kMaxHarm]{};
-    int stage_of[kMaxHarm]{};
-    std::vector<int> mvals;
-    long long dstride = 0, pstride = 0;
-    float cuts[kMaxStages]{};
-
-    // work buffers
-    int chunk = 1;
-    int plane_split = 0;
-    int fused_sum = 0;
-    int overlap = 1;          // sum of group k on stream2 while group k+1 is transformed
-    cudaStream_t stream2 = nullptr;
-    float* planes2 = nullptr; // second plane buffer for the overlap
-    cudaEvent_t ev_fork = nullptr, ev_plane[2] = {nullptr, nullptr}, ev_sum[2] = {nullptr, nullptr};
-    bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
-    int hsum_tiled = 1;
-    int tile_floats = 0;
-    float2* dbuf = nullptr;
-    float* planes = nullptr;
-    SegDesc* d_segs = nullptr;
-    SegDesc* h_segs = nullptr;  // pinned
-    long long segs_cap = 0;
-    RawCand* d_cands = nullptr;
-    unsigned long long* d_ncand = nullptr;
-    unsigned long long* h_ncand = nullptr;  // pinned
-    long long cand_cap = 0;
-
-    std::map<unsigned, WhitenPlanDev> wplans;
-    std::map<long long, cufftHandle> fftplans;
-    std::vector<TrialBuf> trials;
-
-    std::vector<accel_candidate> results;
-    unsigned long long last_raw = 0;
-
-    // accounting
-    bool profiling = false;
-    struct Ev { int kind; cudaEvent_t a, b; };
-    std::vector<Ev> pending;
-    std::vector<cudaEvent_t> evpool;
-    accel_stats stats{};
-    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // bracket each search call
-};
-
-namespace {
+namespace accel {
 
 int ensure_device(accel_ctx* c) {
     CK(cudaSetDevice(c->device));
@@ -481,12 +413,25 @@ int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec) {
     cufftHandle plan;
     auto it = c->fftplans.find(n);
     if (it == c->fftplans.end()) {
+        // bounded plan cache: drop the least recently used plan
+        if (c->fftplans.size() >= 64) {
+            auto lru = std::min_element(c->fftplan_use.begin(), c->fftplan_use.end(),
+                                        [](const std::pair<const long long, long long>& a,
+                                           const std::pair<const long long, long long>& b) {
+                                            return a.second < b.second;
+                                        });
+            CK(cudaStreamSynchronize(c->stream));
+            cufftDestroy(c->fftplans[lru->first]);
+            c->fftplans.erase(lru->first);
+            c->fftplan_use.erase(lru);
+        }
         if (cufftPlan1d(&plan, (int)n, CUFFT_R2C, 1) != CUFFT_SUCCESS)
             return set_err(ACCEL_ERR_CUDA, "cufftPlan1d(%lld, R2C) failed", n);
         c->fftplans[n] = plan;
     } else {
         plan = it->second;
     }
+    c->fftplan_use[n] = ++c->fftplan_clock;
     ProfScope ps(c, K_RFFT, 1);
     if (cufftSetStream(plan, c->stream) != CUFFT_SUCCESS)
         return set_err(ACCEL_ERR_CUDA, "cufftSetStream failed");
@@ -502,7 +447,7 @@ int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec) {
 // plane is stored and, with do_sum, k_hsum sums them (the stage API).
 int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float* stage_out,
               const float2* dh_in, float* planes_out, bool do_prep, bool do_plane, bool do_sum,
-              bool fused = false, cudaStream_t sum_stream = nullptr) {
+              bool fused, cudaStream_t sum_stream) {
     if (!sum_stream) sum_stream = c->stream;
     float2* dbuf = dh_in ? const_cast<float2*>(dh_in) : c->dbuf;
     float* planes = planes_out ? planes_out : c->planes;
@@ -750,7 +695,7 @@ void free_ctx(accel_ctx* c) {
     delete c;
 }
 
-}  // namespace
+}  // namespace accel
 
 namespace accel {
 int set_error(int code, const char* fmt, ...) {
@@ -949,6 +894,16 @@ int accel_set_power_cuts(accel_ctx* c, const float* cuts) {
     for (int s = 0; s < c->nstages; s++) c->cuts[s] = cuts[s];
     return ACCEL_OK;
 }
+
+}  // extern "C"
+
+namespace accel {
+double sigma_of_power_host(double power, int numharm, double numindep) {
+    return sigma_of_power(power, numharm, numindep);
+}
+}  // namespace accel
+
+extern "C" {
 
 double accel_power_cut(double sigma, int numharm, double numindep) {
     return power_cut(sigma, numharm, numindep);

@@ -1,0 +1,107 @@
+// context.h -- the search context (accel_ctx) and the host-side driver
+// functions shared by api.cu (the accel_* C ABI) and server.cu (the
+// request server).  Internal to libaccelsearch.so.
+#pragma once
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/accelsearch.h"
+#include "accel_internal.h"
+
+namespace accel {
+
+struct WhitenPlanDev {
+    int nb = 0, maxlen = 0;
+    int* d_start = nullptr;
+    int* d_len = nullptr;
+    double* d_med = nullptr;
+};
+
+struct TrialBuf {
+    long long n = 0;
+    float* series = nullptr;
+    float2* spec = nullptr;
+};
+
+}  // namespace accel
+
+using namespace accel;  // internal header: the context is written in the library's own types
+
+struct accel_ctx {
+    accel_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int uselen = 0, nh = 0, nstages = 0, numzs0 = 0, zlo0 = 0;
+
+    // bank
+    BankHarmDev bh[kMaxHarm]{};
+    BankHarmDev* d_bh = nullptr;
+    void* bank_mem = nullptr;
+    int ntpl = 0;
+    float2* tw = nullptr;
+
+    // plan
+    HarmPlan hp[kMaxHarm]{};
+    int stage_of[kMaxHarm]{};
+    std::vector<int> mvals;
+    long long dstride = 0, pstride = 0;
+    float cuts[kMaxStages]{};
+
+    // work buffers
+    int chunk = 1;
+    int plane_split = 0;
+    int fused_sum = 0;
+    int overlap = 1;          // sum of group k on stream2 while group k+1 is transformed
+    cudaStream_t stream2 = nullptr;
+    float* planes2 = nullptr; // second plane buffer for the overlap
+    cudaEvent_t ev_fork = nullptr, ev_plane[2] = {nullptr, nullptr}, ev_sum[2] = {nullptr, nullptr};
+    bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
+    int hsum_tiled = 1;
+    int tile_floats = 0;
+    float2* dbuf = nullptr;
+    float* planes = nullptr;
+    SegDesc* d_segs = nullptr;
+    SegDesc* h_segs = nullptr;  // pinned
+    long long segs_cap = 0;
+    RawCand* d_cands = nullptr;
+    unsigned long long* d_ncand = nullptr;
+    unsigned long long* h_ncand = nullptr;  // pinned
+    long long cand_cap = 0;
+
+    std::map<unsigned, WhitenPlanDev> wplans;
+    std::map<long long, cufftHandle> fftplans;
+    std::map<long long, long long> fftplan_use;  // last use of each plan (LRU)
+    long long fftplan_clock = 0;
+    std::vector<TrialBuf> trials;
+
+    std::vector<accel_candidate> results;
+    unsigned long long last_raw = 0;
+
+    // accounting
+    bool profiling = false;
+    struct Ev { int kind; cudaEvent_t a, b; };
+    std::vector<Ev> pending;
+    std::vector<cudaEvent_t> evpool;
+    accel_stats stats{};
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // bracket each search call
+};
+
+namespace accel {
+
+int ensure_device(accel_ctx* c);
+int ensure_segs(accel_ctx* c, long long n);
+int do_whiten(accel_ctx* c, float2* spec, unsigned numbins);
+int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec);
+int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float* stage_out,
+              const float2* dh_in, float* planes_out, bool do_prep, bool do_plane, bool do_sum,
+              bool fused = false, cudaStream_t sum_stream = nullptr);
+void prof_collect(accel_ctx* c);
+double sigma_of_power_host(double power, int numharm, double numindep);
+
+}  // namespace accel

@@ -42,6 +42,19 @@ class Candidate(C.Structure):
                 ("numharm", C.c_int), ("power", C.c_float), ("sigma", C.c_float)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("fftlen", C.c_int),
+                ("numharm", C.c_int), ("sigma", C.c_double), ("chunk_segments", C.c_int),
+                ("device", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
+                ("completed", C.c_longlong), ("queued", C.c_longlong), ("active", C.c_longlong),
+                ("bytes_in_use", C.c_double), ("cells", C.c_longlong), ("gpu_ms", C.c_double),
+                ("admit_ms", C.c_double), ("group_ms", C.c_double)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("chunk_segments", C.c_int), ("plane_split", C.c_int), ("fused_sum", C.c_int),
                 ("hsum_rowwise", C.c_int), ("serial_sum", C.c_int),
@@ -97,6 +110,16 @@ SIGNATURES = {
     "accel_sum_harmonics": (C.c_int, [_vp, _vp, _llp, C.c_int, _vp, _llp]),
     "accel_layout": (C.c_int, [_vp, _llp, _llp, _llp, _llp, C.POINTER(C.c_int)]),
     "accel_bank_spectra": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "accel_whiten_noalloc": (C.c_int, [_vp, _ll, C.c_int, C.c_int, _vp]),
+    "accel_server_config_init": (None, [C.POINTER(ServerConfig)]),
+    "accel_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "accel_server_destroy": (C.c_int, [_vp]),
+    "accel_server_submit": (C.c_int, [_vp, _vp, _ll, C.c_double, C.c_int, _llp]),
+    "accel_server_wait": (C.c_int, [_vp, _ll, C.c_double, C.POINTER(C.c_int)]),
+    "accel_server_result": (C.c_int, [_vp, _ll, C.POINTER(Candidate), _ll, _llp,
+                                      C.POINTER(C.c_double)]),
+    "accel_server_release": (C.c_int, [_vp, _ll]),
+    "accel_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
 }
 
 _lib = None

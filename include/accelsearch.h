@@ -215,6 +215,56 @@ int  accel_layout(const accel_ctx *ctx, long long *dhalf_stride, long long *dhal
 /* Copy of the template bank: kstd [numzs][L_h] and fold [numzs][L_h]. */
 int  accel_bank_spectra(const accel_ctx *ctx, int h, accel_complex *kstd, accel_complex *fold);
 
+/* ------------------------------------------------------------------ serving */
+/* A request server with continuous batching (no counterpart in the
+ * reference, whose driver searches one trial per process run).  A worker
+ * thread admits requests in arrival order while their device memory (series
+ * and spectrum, 12 bytes per sample) fits hbm_budget_bytes, transforms and
+ * whitens them, and fills each launch group with the next steps of every
+ * active request of one template bank (one bank per zmax, built on first
+ * use), round-robin: a request admitted while others are in flight is
+ * searched alongside them from the next group on.  A request's candidates
+ * do not depend on what it was batched with. */
+typedef struct accel_server accel_server;
+
+typedef struct accel_server_config {
+    double hbm_budget_bytes;  /* device memory for admitted requests (150e9)  */
+    int max_active;           /* requests searched at once (0: no limit)       */
+    int fftlen;               /* fundamental segment length of every bank      */
+    int numharm;              /* harmonics summed                              */
+    double sigma;             /* candidate threshold                           */
+    int chunk_segments;       /* steps per launch group (0: 128)               */
+    int device;
+    int reserved[8];
+} accel_server_config;
+
+typedef struct accel_server_stats {
+    long long submitted, admitted, completed, queued, active;
+    double bytes_in_use;      /* budgeted bytes of the admitted requests       */
+    long long cells;          /* fundamental f-fdot cells searched             */
+    double gpu_ms;            /* CUDA-event time of the launch groups          */
+    double admit_ms;          /* worker time admitting (copy, R2C, whitening)  */
+    double group_ms;          /* worker time running launch groups             */
+} accel_server_stats;
+
+void accel_server_config_init(accel_server_config *cfg);
+int  accel_server_create(const accel_server_config *cfg, accel_server **out);
+/* Finishes every submitted request, then frees the server. */
+int  accel_server_destroy(accel_server *srv);
+/* Queue one trial of nsamples float32 samples (host memory, read when the
+ * request is admitted: keep it valid until the request completes).  A
+ * request larger than the whole budget fails with ACCEL_ERR_BUDGET. */
+int  accel_server_submit(accel_server *srv, const float *series, long long nsamples, double dt,
+                         int zmax, long long *id);
+/* Wait up to timeout_s (< 0: forever); *done = 1 once the request finished. */
+int  accel_server_wait(accel_server *srv, long long id, double timeout_s, int *done);
+/* Candidates of a finished request (sorted by step, numharm, z, r) and its
+ * latency from submission to completion. */
+int  accel_server_result(accel_server *srv, long long id, accel_candidate *out, long long cap,
+                         long long *n, double *latency_ms);
+int  accel_server_release(accel_server *srv, long long id);
+int  accel_server_get_stats(accel_server *srv, accel_server_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

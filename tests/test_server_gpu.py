@@ -1,0 +1,79 @@
+"""The continuous-batching request server (accel_server_*) on the GPU."""
+import time
+
+import numpy as np
+import pytest
+
+from gpu_accelsearch_gb300.synth import synth_series
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+DT = 64e-6
+FIELDS = ["step", "r", "z", "numharm", "power", "sigma"]
+
+
+def same(a, b):
+    return len(a) == len(b) and all(np.array_equal(a[f], b[f]) for f in FIELDS)
+
+
+def test_alone_equals_mixed_and_context_path():
+    from gpu_accelsearch_gb300.search import AccelSearch
+    from gpu_accelsearch_gb300.serving import Server
+    a = synth_series(1 << 18, seed=1, signals=[(0.05, 20000.25, 40.0)])
+    others = [(synth_series(1 << 17, seed=2, signals=[(0.1, 9000.5, -30.0)]), 100),
+              (synth_series(1 << 18, seed=3), 50),
+              (synth_series(1 << 16, seed=4, signals=[(0.2, 3000.0, 10.0)]), 200)]
+    with Server(hbm_budget_bytes=2e9, fftlen=2048, numharm=4, chunk_segments=16) as srv:
+        rid = srv.submit(a, DT, 50)
+        assert srv.wait(rid, 60)
+        alone, _ = srv.result(rid)
+        ids = [srv.submit(x, DT, z) for x, z in others[:2]]
+        rid2 = srv.submit(a, DT, 50)
+        ids.append(srv.submit(*others[2][:1], DT, others[2][1]))
+        for i in ids + [rid2]:
+            assert srv.wait(i, 60)
+        mixed, _ = srv.result(rid2)
+        st = srv.stats()
+        assert st["completed"] == 5 and st["active"] == 0 and st["bytes_in_use"] == 0
+    assert len(alone) > 0
+    assert same(alone, mixed)
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048) as s:
+        s.search([a], DT)
+        assert same(alone, s.candidates())
+
+
+def test_budget_admission_and_rejection():
+    from gpu_accelsearch_gb300.native import AccelError
+    from gpu_accelsearch_gb300.serving import Server
+    n = 1 << 17
+    per = 4.0 * n + 8.0 * (n // 2 + 1)
+    with Server(hbm_budget_bytes=2.5 * per, fftlen=2048, numharm=4, chunk_segments=8) as srv:
+        xs = [synth_series(n, seed=10 + i) for i in range(5)]
+        ids = [srv.submit(x, DT, 50) for x in xs]
+        for i in ids:
+            assert srv.wait(i, 60)
+        st = srv.stats()
+        assert st["completed"] == 5 and st["bytes_in_use"] == 0
+        with pytest.raises(AccelError) as e:
+            srv.submit(synth_series(1 << 19, seed=99), DT, 50)
+        assert e.value.code == -6
+
+
+def test_continuous_batching_short_request_overtakes():
+    from gpu_accelsearch_gb300.serving import Server
+    long_x = synth_series(1 << 23, seed=20)
+    short_x = synth_series(1 << 15, seed=21)
+    with Server(hbm_budget_bytes=4e9, fftlen=2048, numharm=4, chunk_segments=16) as srv:
+        assert srv.wait(srv.submit(short_x, DT, 50), 60)  # bank built before the measurement
+        lid = srv.submit(long_x, DT, 50)
+        while srv.stats()["active"] == 0:  # wait until the long request is being searched
+            time.sleep(0.001)
+        sid = srv.submit(short_x, DT, 50)
+        long_running = not srv.wait(lid, 0.0)
+        assert srv.wait(sid, 60)
+        short_done_first = not srv.wait(lid, 0.0)
+        assert srv.wait(lid, 300)
+        _, lat_long = srv.result(lid)
+        _, lat_short = srv.result(sid)
+    assert long_running and short_done_first
+    assert lat_short < lat_long
