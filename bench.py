@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--precision-seeds", type=int, default=100,
+                    help="seeds of the FP16-template precision report (0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=5.0,
                     help="duration of the Poisson arrival process of the serving leg (0: skip)")
     return ap.parse_args()
@@ -211,6 +213,84 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
                         "continuous batching (accel_server)"}
 
 
+# --------------------------------------------------------------- precision
+def precision_report(seeds: int, device: int):
+    """FP16 folded templates (scaled per template) against FP32 templates
+    and the FP64 oracle on the single-trial configuration: N = 2^22, three
+    injected signals per seed (r in [1e4, 1e6], z in [-150, 150], amplitude
+    in [0.02, 0.1]), zmax = 200, 8 harmonics, L = 8192, sigma = 6."""
+    import torch
+    from gpu_accelsearch_gb300.search import AccelSearch
+    from oracle import oracle as O
+    n = 1 << 22
+    s32 = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, device=device)
+    s16 = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, template_fp16=True, device=device)
+    U, half = s32.uselen, s32.uselen // 2
+    rec16 = rec32 = inj = 0
+    agree = tot32 = 0
+    worst_err, errs = 0.0, []
+    orc = None
+    for seed in range(seeds):
+        rng = np.random.default_rng(9000 + seed)
+        sigs = [(float(rng.uniform(0.02, 0.1)), float(rng.uniform(1e4, 1e6)), float(rng.uniform(-150, 150)))
+                for _ in range(3)]
+        x = device_series(torch, [n], [None], seed=5000 + seed)[0]
+        t = torch.arange(n, device="cuda", dtype=torch.float64) / n
+        for amp, r0, z in sigs:
+            x += (amp * torch.cos(2 * np.pi * (r0 * t + 0.5 * z * t * t))).float()
+        torch.cuda.synchronize()
+        res = []
+        for s in (s32, s16):
+            s.search([x.data_ptr()], DT, on_device=True, nsamples=[n])
+            res.append(s.candidates())
+        c32, c16 = res
+        k32 = {(int(c["step"]), float(c["r"]), float(c["z"]), int(c["numharm"])) for c in c32}
+        k16 = {(int(c["step"]), float(c["r"]), float(c["z"]), int(c["numharm"])) for c in c16}
+        agree += len(k32 & k16)
+        tot32 += len(k32)
+        for amp, r0, z in sigs:
+            inj += 1
+            for c, cnt in ((c32, 0), (c16, 1)):
+                hit = np.any((np.abs(c["r"] - (r0 + z / 2)) <= 2.0) & (np.abs(c["z"] - z) <= 4.0))
+                if cnt == 0:
+                    rec32 += int(hit)
+                else:
+                    rec16 += int(hit)
+        if seed < 2:  # power error against the FP64 oracle on the step holding the first signal
+            if orc is None:
+                orc = O.Oracle(ZMAX, NUMHARM, U)
+            spec = torch.fft.rfft(x.double()).to(torch.complex64)[: n // 2].cpu().numpy()
+            w = O.deredden(spec)
+            rlo = int(np.floor(np.float32(n) * np.float32(DT)))
+            step = max(0, int((sigs[0][1] + sigs[0][2] / 2 - rlo) // half) - 1)
+            startr = rlo + step * half
+            d = torch.from_numpy(w.view(np.float32).copy()).cuda()
+            dh = torch.zeros(s16.dhalf_stride * 2, dtype=torch.float32, device="cuda")
+            pl = torch.zeros(s16.plane_stride, dtype=torch.float32, device="cuda")
+            s16.prepare_segments(d.data_ptr(), w.size, [startr], dh.data_ptr())
+            s16.power_planes(dh.data_ptr(), 1, pl.data_ptr())
+            P = pl.cpu().numpy()
+            for h, hi in enumerate(s16.harmonics):
+                p64 = orc.harmonic_plane(w, float(startr), h)
+                nz, nr = p64.shape
+                g = P[s16.plane_off[h]: s16.plane_off[h] + nz * s16.plane_row[h]].reshape(
+                    nz, s16.plane_row[h])[:, :nr]
+                e = np.abs(g - p64) / np.maximum(p64, 1.0)
+                worst_err = max(worst_err, float(e.max()))
+                errs.append(float(e.mean()))
+    s32.close()
+    s16.close()
+    if orc is not None:
+        orc.close()
+    return {"seeds": seeds, "injected": inj, "recovered_fp32": rec32, "recovered_fp16": rec16,
+            "recovery_rate_fp16": rec16 / max(inj, 1), "recovery_rate_fp32": rec32 / max(inj, 1),
+            "candidate_agreement_fp16_vs_fp32": agree / max(tot32, 1),
+            "max_rel_power_error_vs_fp64": worst_err,
+            "mean_rel_power_error_vs_fp64": float(np.mean(errs)) if errs else None,
+            "error_metric": "|P - P64| / max(P64, 1) over every plane of one step per seed (2 seeds)",
+            "workload": "N=2^22, 3 injected signals per seed, zmax=200, 8 harmonics, L=8192, sigma=6"}
+
+
 # ------------------------------------------------------------ cpu baseline
 def cpu_baseline(seconds: float):
     """The oracle (FP64 restatement of the reference path) on a bounded
@@ -304,6 +384,7 @@ def run_ours(args):
 
     lengths, sigs = make_batch(args.trials, seed=1000 + rank)
     series = device_series(torch, lengths, sigs, seed=2000 + rank)
+    torch.cuda.synchronize()
     ptrs = [x.data_ptr() for x in series]
     from gpu_accelsearch_gb300.search import autotune
     tuned = None
@@ -448,6 +529,7 @@ def run_ours(args):
                    "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
     cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
     serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
+    precision = precision_report(args.precision_seeds, local) if args.precision_seeds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
@@ -470,6 +552,7 @@ def run_ours(args):
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "candidates_per_step": ncand,
         "serving": serving,
+        "precision_fp16": precision,
     }
     print(json.dumps(line), flush=True)
     s.close()

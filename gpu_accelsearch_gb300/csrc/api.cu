@@ -346,7 +346,7 @@ int alloc_work(accel_ctx* c) {
     CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * chunk));
     CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * chunk));
     CK(cudaMalloc(&c->planes2, sizeof(float) * c->pstride * chunk));
-    CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    CK(cudaStreamCreate(&c->stream2));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     for (int b = 0; b < 2; b++) {
         CK(cudaEventCreateWithFlags(&c->ev_plane[b], cudaEventDisableTiming));
@@ -754,7 +754,9 @@ int accel_create(const accel_config* cfg, accel_ctx** out) {
     c->uselen = U;
     int rc = ensure_device(c);
     if (!rc) {
-        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        // a blocking stream: ordered with the legacy default stream, where
+        // callers (PyTorch by default) produce the inputs they pass in
+        cudaError_t e = cudaStreamCreate(&c->stream);
         if (e != cudaSuccess) rc = set_err(ACCEL_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
         c->own_stream = true;
     }
@@ -792,7 +794,7 @@ int accel_set_stream(accel_ctx* c, void* s) {
     if (s) {
         c->stream = (cudaStream_t)s;
     } else {
-        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreate(&c->stream));
         c->own_stream = true;
     }
     return ACCEL_OK;

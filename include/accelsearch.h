@@ -109,7 +109,8 @@ const char *accel_last_error(void);
 void accel_config_init(accel_config *cfg);
 int  accel_create(const accel_config *cfg, accel_ctx **out);
 int  accel_destroy(accel_ctx *ctx);
-/* Run all further work of ctx on this cudaStream_t (NULL: the context's own). */
+/* Run all further work of ctx on this cudaStream_t (NULL: the context's own,
+ * a blocking stream ordered with the legacy default stream). */
 int  accel_set_stream(accel_ctx *ctx, void *cuda_stream);
 int  accel_synchronize(accel_ctx *ctx);
 /* Time every kernel with CUDA events on the context's stream (1) or not (0). */

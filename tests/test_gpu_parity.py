@@ -262,3 +262,50 @@ def test_many_candidates_match_oracle(S, trial, orc):
     g = _keyset(gpu, rlo, S.uselen // 2, -50)
     assert len(g) > 2000
     assert _keyset(o_hi, 0, 0, 0) <= g <= _keyset(o_lo, 0, 0, 0)
+
+
+def test_fp16_templates_within_stated_tolerance(trial, orc):
+    # FP16 folded templates, scaled per template: power error stated as
+    # |P - P64| / max(P64, 1) < 5e-3 (FP16 keeps 11 mantissa bits), and the
+    # injected signal still the strongest cell
+    from gpu_accelsearch_gb300.search import AccelSearch
+    w = trial["w"]
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048, template_fp16=True) as s:
+        startr = [16 + 957 * 20]
+        d = dev(w)
+        nseg = 1
+        dh = torch.zeros(nseg * s.dhalf_stride * 2, dtype=torch.float32, device="cuda")
+        pl = torch.zeros(nseg * s.plane_stride, dtype=torch.float32, device="cuda")
+        s.prepare_segments(d.data_ptr(), w.size, startr, dh.data_ptr())
+        s.power_planes(dh.data_ptr(), nseg, pl.data_ptr())
+        P = pl.cpu().numpy()
+        worst = 0.0
+        for h, hi in enumerate(s.harmonics):
+            p64 = orc.harmonic_plane(w, float(startr[0]), h)
+            nz, nr = p64.shape
+            g = P[s.plane_off[h]: s.plane_off[h] + nz * s.plane_row[h]].reshape(nz, s.plane_row[h])[:, :nr]
+            worst = max(worst, (np.abs(g - p64) / np.maximum(p64, 1.0)).max())
+        assert worst < 5e-3, worst
+        s.search_spectra([d.data_ptr()], [w.size], [trial["rlo"]])
+        c = s.candidates()
+    best = c[np.argmax(c["power"])]
+    assert abs(best["r"] - 20020.25) <= 1.0 and abs(best["z"] - 40) <= 4
+
+
+def test_inputs_from_pending_torch_kernels(S, trial):
+    # the library's stream is ordered with the legacy default stream: a
+    # series still being produced by torch kernels is read only after them
+    n = trial["n"]
+    S.search([trial["x"]], trial["dt"])
+    want = S.candidates()
+    base = torch.from_numpy(trial["x"]).cuda()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        y = torch.zeros(n, device="cuda")
+        for _ in range(20):  # a queue of kernels ahead of the search
+            y = y * 0.5 + base * 0.5
+        y = y + base * (1.0 - float(1.0 - 0.5 ** 20))  # == base up to rounding
+        S.search([y.data_ptr()], trial["dt"], on_device=True, nsamples=[n])
+        got = S.candidates()
+        assert len(got) == len(want)
+        assert np.allclose(got["power"], want["power"], rtol=1e-3)
