@@ -322,6 +322,8 @@ template <int NH, bool STAGE_OUT>
 __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     extern __shared__ __align__(16) float tsm[];
     __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
+    __shared__ int s_zf[NH], s_c0[NH], s_w4[NH], s_off[NH];
+    __shared__ long long s_rlo2[NH];
     const int seg = blockIdx.z;
     const int z0 = blockIdx.y * kTileZ;
     const int i0 = blockIdx.x * kTileI;
@@ -333,41 +335,60 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     const int i = i0 + tid;
     const bool valid = tid < ni;
 
-    // Rectangles: rows [zf, zl] and 4-aligned columns [c0, c0 + 4*w4) per harmonic.
-    int col[NH];
-    int off = 0;
+    // 1. rectangles (one thread per harmonic): rows [zf, zl], 4-aligned
+    //    columns [c0, c0 + 4 w4), placed one after another in shared memory
+    if (tid == 0) {
+        int off = 0;
+#pragma unroll
+        for (int h = 0; h < NH; h++) {
+            const HarmPlan& H = a.h[h];
+            int rfirst = i0, rlast = i0 + ni - 1, zf = z0, zl = z0 + nz - 1;
+            long long rlo2 = 0;
+            if (h > 0) {
+                rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+                rfirst = (int)(unsigned short)(twice_r_shift(2 * startr + i0, H.p, H.lq) - rlo2);
+                rlast = (int)(unsigned short)(twice_r_shift(2 * startr + i0 + ni - 1, H.p, H.lq) - rlo2);
+                zf = sub_row(a.zlo0 + kDz * z0, H);
+                zl = sub_row(a.zlo0 + kDz * (z0 + nz - 1), H);
+            }
+            const int c0 = rfirst & ~3;
+            const int w4 = ((rlast - c0) >> 2) + 1;
+            s_zf[h] = zf;
+            s_c0[h] = c0;
+            s_w4[h] = w4;
+            s_off[h] = off;
+            s_rlo2[h] = rlo2;
+            off += 4 * (zl - zf + 1) * w4;
+        }
+    }
+    __syncthreads();
+    // 2. copies (warps over rows, lanes over 16-byte chunks) and row table
 #pragma unroll
     for (int h = 0; h < NH; h++) {
         const HarmPlan& H = a.h[h];
-        int rfirst, rlast, zf, zl, mycol;
-        if (h == 0) {
-            rfirst = i0;
-            rlast = i0 + ni - 1;
-            zf = z0;
-            zl = z0 + nz - 1;
-            mycol = i;
-        } else {
-            const long long rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
-            rfirst = (int)(unsigned short)(twice_r_shift(2 * startr + i0, H.p, H.lq) - rlo2);
-            rlast = (int)(unsigned short)(twice_r_shift(2 * startr + i0 + ni - 1, H.p, H.lq) - rlo2);
-            mycol = valid ? (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - rlo2) : rfirst;
-            zf = sub_row(a.zlo0 + kDz * z0, H);
-            zl = sub_row(a.zlo0 + kDz * (z0 + nz - 1), H);
-        }
-        const int c0 = rfirst & ~3;
-        const int w4 = ((rlast - c0) >> 2) + 1;  // 16-byte chunks per row
-        col[h] = off + (mycol - c0);
+        const int zf = s_zf[h], w4 = s_w4[h], off = s_off[h];
         if (tid < nz) {
-            const int zr = tid;
-            const int r = (h == 0) ? zr : sub_row(a.zlo0 + kDz * (z0 + zr), H) - zf;
-            s_row[h][zr] = 4 * w4 * r;
+            const int r = (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), H) - zf;
+            s_row[h][tid] = off + 4 * w4 * r;
         }
-        const int nzr = zl - zf + 1;
-        const float* src = P + H.poff + (long long)zf * H.prow + c0;
+        const int nzr = (h == 0) ? nz : sub_row(a.zlo0 + kDz * (z0 + nz - 1), H) - zf + 1;
+        const float* src = P + H.poff + (long long)zf * H.prow + s_c0[h];
         for (int r = tid >> 5; r < nzr; r += kTileI / 32)
             for (int c = tid & 31; c < w4; c += 32)
                 cp_async16(tsm + off + 4 * (r * w4 + c), src + (long long)r * H.prow + 4 * c);
-        off += 4 * nzr * w4;
+    }
+    // 3. this thread's column in every rectangle
+    int col[NH];
+#pragma unroll
+    for (int h = 0; h < NH; h++) {
+        if (h == 0) {
+            col[h] = tid;
+        } else {
+            const HarmPlan& H = a.h[h];
+            const int rind = valid ? (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - s_rlo2[h])
+                                   : s_c0[h];
+            col[h] = rind - s_c0[h];
+        }
     }
     float cut[kMaxStages];
 #pragma unroll
@@ -375,22 +396,34 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     cp_async_wait_all();
     __syncthreads();
 
+    // 4. sums in the reference's harmonic order; one warp vote over all
+    //    stage tests, the per-stage appends only when some lane hit
 #pragma unroll 2
     for (int zr = 0; zr < nz; zr++) {
         const int z = z0 + zr;
-        float s = 0.f;
+        float s = 0.f, sst[kMaxStages];
+        bool any = false;
 #pragma unroll
         for (int h = 0; h < NH; h++) {
             const float v = tsm[s_row[h][zr] + col[h]];
             s = (h == 0) ? v : s + v;
             const int st = stage_after(h);  // folds to a constant once h is unrolled
             if (st >= 0) {
+                sst[st] = s;
+                any |= s > cut[st];
                 if constexpr (STAGE_OUT) {
                     if (valid)
                         a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
                 }
-                append_candidates(valid && s > cut[st], a.seg_base + seg, i, z, h + 1, s, a.cands,
-                                  a.ncand, a.cap);
+            }
+        }
+        if (__any_sync(0xffffffffu, valid && any)) {
+#pragma unroll
+            for (int h = 0; h < NH; h++) {
+                const int st = stage_after(h);
+                if (st >= 0)
+                    append_candidates(valid && sst[st] > cut[st], a.seg_base + seg, i, z, h + 1, sst[st],
+                                      a.cands, a.ncand, a.cap);
             }
         }
     }
