@@ -207,6 +207,8 @@ int build_bank(accel_ctx* c) {
             n++;
         }
     }
+    if (tb > 65535)  // the plane kernels index templates by blockIdx.y
+        return set_err(ACCEL_ERR_UNSUPPORTED, "template bank of %d rows exceeds 65535", tb);
     c->nh = n;
     c->ntpl = tb;
     c->nstages = stages;
@@ -1096,7 +1098,15 @@ int accel_bank_spectra(const accel_ctx* c, int h, accel_complex* kstd, accel_com
     size_t n = (size_t)b.numzs * 2 * b.M;
     CK(cudaSetDevice(c->device));
     if (kstd) CK(cudaMemcpy(kstd, b.kstd, sizeof(float2) * n, cudaMemcpyDeviceToHost));
-    if (fold) CK(cudaMemcpy(fold, b.fold, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+    if (fold) {
+        // the device copy is scaled by 1/L (exact); A and B are returned unscaled
+        CK(cudaMemcpy(fold, b.fold, sizeof(float2) * n, cudaMemcpyDeviceToHost));
+        const float L = 2.0f * (float)b.M;
+        for (size_t i = 0; i < n; i++) {
+            fold[i].x *= L;
+            fold[i].y *= L;
+        }
+    }
     return ACCEL_OK;
 }
 

@@ -14,8 +14,8 @@
 //
 // Outputs per harmonic h (numzs_h templates of length L_h = 2 M_h):
 //   kstd[z][0..L)   the template spectrum K = FFT_L(k) (forward, unnormalised)
-//   fold[z][0..M)   A[k] = conj K[k] + conj K[k+M]
-//   fold[z][M..2M)  B[k] = (conj K[k] - conj K[k+M]) exp(+2 pi i k / L)
+//   fold[z][0..M)   A[k] / L, A[k] = conj K[k] + conj K[k+M]
+//   fold[z][M..2M)  B[k] / L, B[k] = (conj K[k] - conj K[k+M]) exp(+2 pi i k / L)
 // so that, for segment data repeated with period M (spread x2), the inverse
 // L-point transform of D.conj(K) has even outputs IFFT_M(D.A) and odd
 // outputs IFFT_M(D.B).
@@ -202,11 +202,14 @@ __global__ void k_template_dft(const BankHarmDev* __restrict__ hd, int nh, const
     float2* kstd = H.kstd + (size_t)j * L;
     kstd[k] = make_float2((float)(ser + sor), (float)(sei + soi));
     kstd[k + H.M] = make_float2((float)(ser - sor), (float)(sei - soi));
+    // folded spectra scaled by 1/L (a power of two: exact), so that the
+    // plane kernels' |y|^2 is already the normalised power |y / L|^2
+    const double inv_l = 1.0 / L;
     float2* fold = H.fold + (size_t)j * 2 * H.M;
-    fold[k] = make_float2((float)(2.0 * ser), (float)(-2.0 * sei));
+    fold[k] = make_float2((float)(2.0 * ser * inv_l), (float)(-2.0 * sei * inv_l));
     // So * w, then conjugate, times 2
     double qr = sor * cw - soi * sw, qi = sor * sw + soi * cw;
-    fold[H.M + k] = make_float2((float)(2.0 * qr), (float)(-2.0 * qi));
+    fold[H.M + k] = make_float2((float)(2.0 * qr * inv_l), (float)(-2.0 * qi * inv_l));
 }
 
 // FP16 copy of the folded bank, scaled per template by its largest

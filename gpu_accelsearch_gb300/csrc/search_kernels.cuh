@@ -125,15 +125,15 @@ __device__ __forceinline__ void plane_transform(const HarmPlan& H, const float2*
     fft_run<M, +1, NB>(x, sm + (SPLIT ? half * PM : 0), tw, t);
 }
 
-// Stage the row's powers |y|^2 / L^2 for columns [0, wmax) in shared memory
-// (interleaving even and odd outputs) and return the float view.
+// Stage the row's powers for columns [0, wmax) in shared memory
+// (interleaving even and odd outputs) and return the float view.  The
+// folded templates carry the 1/L normalisation, so |y|^2 is the power.
 template <int M, bool SPLIT>
 __device__ __forceinline__ float* stage_row_powers(const HarmPlan& H, unsigned char* smem_raw,
                                                    const float2 (&x)[PlaneShape<SPLIT, M>::NB][16],
                                                    int t, int half) {
     constexpr int T = M / 16;
     constexpr int NB = PlaneShape<SPLIT, M>::NB;
-    const float scale = 1.0f / (4.0f * (float)M * (float)M);  // 1 / L^2, exact
     float* pw = reinterpret_cast<float*>(smem_raw);
     const int half_w = H.wmax >> 1;
     __syncthreads();  // every thread has finished reading the transform buffers
@@ -143,8 +143,7 @@ __device__ __forceinline__ float* stage_row_powers(const HarmPlan& H, unsigned c
         if (i2 >= 0 && i2 < half_w) {
 #pragma unroll
             for (int nb = 0; nb < NB; nb++)
-                pw[2 * i2 + (SPLIT ? half : nb)] =
-                    fmaf(x[nb][e].x, x[nb][e].x, x[nb][e].y * x[nb][e].y) * scale;
+                pw[2 * i2 + (SPLIT ? half : nb)] = fmaf(x[nb][e].x, x[nb][e].x, x[nb][e].y * x[nb][e].y);
         }
     }
     __syncthreads();
@@ -157,13 +156,15 @@ __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLI
     constexpr int T = M / 16;
     constexpr int NB = PlaneShape<SPLIT, M>::NB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int item = blockIdx.x;
+    // segments vary fastest across the grid, so that the CTAs resident at
+    // one time share a few templates (read from DRAM once, then from L2)
+    const int item = blockIdx.y;
     int hi = 0;
 #pragma unroll 1
     while (hi + 1 < a.nh && item >= a.h[hi + 1].zbase) hi++;
     const HarmPlan& H = a.h[hi];
     const int z = item - H.zbase;
-    const int seg = blockIdx.y;
+    const int seg = blockIdx.x;
     const int half = SPLIT ? (int)(threadIdx.x / T) : 0;
     const int t = SPLIT ? (int)(threadIdx.x % T) : (int)threadIdx.x;
     float2 x[NB][16];
@@ -172,7 +173,6 @@ __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLI
     // straight from registers: even/odd pairs as 8-byte stores (one thread
     // holds both), or single floats interleaved by the two halves
     float* row = a.planes + (long long)seg * a.pstride + H.poff + (long long)z * H.prow;
-    const float scale = 1.0f / (4.0f * (float)M * (float)M);  // 1 / L^2, exact
     const int half_w = H.wmax >> 1;
 #pragma unroll
     for (int e = 0; e < 16; e++) {
@@ -180,11 +180,11 @@ __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLI
         if (i2 >= 0 && i2 < half_w) {
             if constexpr (NB == 2) {
                 float2 p;
-                p.x = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y) * scale;
-                p.y = fmaf(x[1][e].x, x[1][e].x, x[1][e].y * x[1][e].y) * scale;
+                p.x = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y);
+                p.y = fmaf(x[1][e].x, x[1][e].x, x[1][e].y * x[1][e].y);
                 *reinterpret_cast<float2*>(row + 2 * i2) = p;
             } else {
-                row[2 * i2 + half] = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y) * scale;
+                row[2 * i2 + half] = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y);
             }
         }
     }
@@ -530,7 +530,7 @@ static int plane_m(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t 
             return -1;
         attr = true;
     }
-    k_plane<M, F16, SPLIT><<<dim3(a.ntpl, nseg), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
+    k_plane<M, F16, SPLIT><<<dim3(nseg, a.ntpl), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
