@@ -322,7 +322,7 @@ template <int NH, bool STAGE_OUT>
 __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     extern __shared__ __align__(16) float tsm[];
     __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
-    __shared__ int s_zf[NH], s_c0[NH], s_w4[NH], s_off[NH];
+    __shared__ int s_zf[NH], s_nzr[NH], s_c0[NH], s_w4[NH], s_off[NH];
     __shared__ long long s_rlo2[NH];
     const int seg = blockIdx.z;
     const int z0 = blockIdx.y * kTileZ;
@@ -335,12 +335,13 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     const int i = i0 + tid;
     const bool valid = tid < ni;
 
-    // 1. rectangles (one thread per harmonic): rows [zf, zl], 4-aligned
-    //    columns [c0, c0 + 4 w4), placed one after another in shared memory
-    if (tid == 0) {
-        int off = 0;
-#pragma unroll
-        for (int h = 0; h < NH; h++) {
+    // 1. rectangles, lane h of warp 0 for harmonic h: rows [zf, zf + nzr),
+    //    4-aligned columns [c0, c0 + 4 w4), placed one after another in
+    //    shared memory (offsets by a warp prefix sum)
+    if (tid < 32) {
+        int size = 0;
+        if (tid < NH) {
+            const int h = tid;
             const HarmPlan& H = a.h[h];
             int rfirst = i0, rlast = i0 + ni - 1, zf = z0, zl = z0 + nz - 1;
             long long rlo2 = 0;
@@ -354,24 +355,30 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
             const int c0 = rfirst & ~3;
             const int w4 = ((rlast - c0) >> 2) + 1;
             s_zf[h] = zf;
+            s_nzr[h] = zl - zf + 1;
             s_c0[h] = c0;
             s_w4[h] = w4;
-            s_off[h] = off;
             s_rlo2[h] = rlo2;
-            off += 4 * (zl - zf + 1) * w4;
+            size = 4 * (zl - zf + 1) * w4;
         }
+        int incl = size;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (tid >= o) incl += v;
+        }
+        if (tid < NH) s_off[tid] = incl - size;
     }
     __syncthreads();
     // 2. copies (warps over rows, lanes over 16-byte chunks) and row table
 #pragma unroll
     for (int h = 0; h < NH; h++) {
         const HarmPlan& H = a.h[h];
-        const int zf = s_zf[h], w4 = s_w4[h], off = s_off[h];
+        const int zf = s_zf[h], w4 = s_w4[h], off = s_off[h], nzr = s_nzr[h];
         if (tid < nz) {
             const int r = (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), H) - zf;
             s_row[h][tid] = off + 4 * w4 * r;
         }
-        const int nzr = (h == 0) ? nz : sub_row(a.zlo0 + kDz * (z0 + nz - 1), H) - zf + 1;
         const float* src = P + H.poff + (long long)zf * H.prow + s_c0[h];
         for (int r = tid >> 5; r < nzr; r += kTileI / 32)
             for (int c = tid & 31; c < w4; c += 32)
