@@ -76,75 +76,73 @@ __global__ void __launch_bounds__(M / 16) k_prep(const PrepArgs a, const float2*
 }
 
 // ----------------------------------------------------------------- plane
-// Two layouts of the same work (chosen per context, see accel_set_tuning):
-//   SPLIT = false: M/16 threads, each carries 16 points of both the even and
-//                  the odd transform (shared twiddles, 128 registers);
-//   SPLIT = true:  M/8 threads, the first half does the even transform, the
-//                  second half the odd one (half the registers per thread,
-//                  twice the warps).
+// Two layouts of the same work (chosen per context, see accel_set_tuning),
+// both M/16 threads carrying 16 points each:
+//   SPLIT = false: each thread carries the even and the odd transform at
+//                  once (two shared buffers, twiddles formed once for both,
+//                  128 registers: 2 CTAs per SM);
+//   SPLIT = true:  the even transform, then the odd one, through one
+//                  shared buffer (fewer registers and half the shared
+//                  memory: 3 CTAs per SM).
 template <bool SPLIT, int M> struct PlaneShape {
-    static constexpr int T = M / 16;
-    static constexpr int THREADS = SPLIT ? M / 8 : M / 16;
-    static constexpr int NB = SPLIT ? 1 : 2;
-    // two CTAs per SM where that leaves 128 registers per thread for the
-    // two-transform layout or 64 for the split one
-    static constexpr int MINB = SPLIT ? (THREADS <= 512 ? 2 : 1) : (THREADS <= 256 ? 2 : 1);
+    static constexpr int THREADS = M / 16;
+    static constexpr int BUFFERS = SPLIT ? 1 : 2;
+    static constexpr int MINB = SPLIT ? (THREADS <= 256 ? 3 : 1) : (THREADS <= 256 ? 2 : 1);
 };
 
-// Multiply the segment spectrum by template z's folded spectrum and run the
-// inverse transform(s).  On return x[nb][e] holds output t + e*T of the even
-// (nb or half 0) / odd (nb or half 1) transform.
+// Template z's folded spectrum (half 0: A, half 1: B) at frequency idx.
+template <int M, bool F16>
+__device__ __forceinline__ float2 fold_at(const HarmPlan& H, int z, int half, int idx) {
+    if constexpr (F16) {
+        float2 w = __half22float2(H.fold16[(size_t)z * 2 * M + half * M + idx]);
+        const float sc = H.f16scale[z];
+        w.x *= sc;
+        w.y *= sc;
+        return w;
+    } else {
+        return __ldg(H.fold + (size_t)z * 2 * M + half * M + idx);
+    }
+}
+
+// Row z of a harmonic's plane for one segment, both transforms at once:
+// multiply the segment spectrum D by the folded template, run the inverse
+// transforms and leave p[e] = (power of even output, power of odd output)
+// at m = t + e*M/16.  The templates carry the 1/L normalisation, so |y|^2
+// is the power.
 template <int M, bool F16, bool SPLIT>
-__device__ __forceinline__ void plane_transform(const HarmPlan& H, const float2* __restrict__ D, int z,
-                                                float2* sm, const float2* __restrict__ tw,
-                                                float2 (&x)[PlaneShape<SPLIT, M>::NB][16], int t,
-                                                int half) {
+__device__ __forceinline__ void plane_powers(const HarmPlan& H, const float2* __restrict__ D, int z,
+                                             float2* sm, const float2* __restrict__ tw, float2 (&p)[16],
+                                             int t) {
+    static_assert(!SPLIT, "the sequential layout stores each transform as it completes");
     constexpr int T = M / 16;
-    constexpr int NB = PlaneShape<SPLIT, M>::NB;
-    constexpr int PM = FftShape<M>::PADDED;
+    float2 x[2][16];
 #pragma unroll
     for (int e = 0; e < 16; e++) {
         const int idx = t + e * T;
         const float2 d = D[idx];
-        if constexpr (F16) {
-            const __half2* f = H.fold16 + (size_t)z * 2 * M;
-            const float sc = H.f16scale[z];
-#pragma unroll
-            for (int nb = 0; nb < NB; nb++) {
-                float2 A = __half22float2(f[(SPLIT ? half : nb) * M + idx]);
-                A.x *= sc;
-                A.y *= sc;
-                x[nb][e] = cmul(d, A);
-            }
-        } else {
-            const float2* f = H.fold + (size_t)z * 2 * M;
-#pragma unroll
-            for (int nb = 0; nb < NB; nb++) x[nb][e] = cmul(d, __ldg(f + (SPLIT ? half : nb) * M + idx));
-        }
+        x[0][e] = cmul(d, fold_at<M, F16>(H, z, 0, idx));
+        x[1][e] = cmul(d, fold_at<M, F16>(H, z, 1, idx));
     }
-    fft_run<M, +1, NB>(x, sm + (SPLIT ? half * PM : 0), tw, t);
+    fft_run<M, +1, 2>(x, sm, tw, t);
+#pragma unroll
+    for (int e = 0; e < 16; e++)
+        p[e] = make_float2(fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y),
+                           fmaf(x[1][e].x, x[1][e].x, x[1][e].y * x[1][e].y));
 }
 
-// Stage the row's powers for columns [0, wmax) in shared memory
-// (interleaving even and odd outputs) and return the float view.  The
-// folded templates carry the 1/L normalisation, so |y|^2 is the power.
-template <int M, bool SPLIT>
+// Stage the row's powers for columns [0, wmax) in shared memory (even and
+// odd outputs interleaved) and return the float view.
+template <int M>
 __device__ __forceinline__ float* stage_row_powers(const HarmPlan& H, unsigned char* smem_raw,
-                                                   const float2 (&x)[PlaneShape<SPLIT, M>::NB][16],
-                                                   int t, int half) {
+                                                   const float2 (&p)[16], int t) {
     constexpr int T = M / 16;
-    constexpr int NB = PlaneShape<SPLIT, M>::NB;
     float* pw = reinterpret_cast<float*>(smem_raw);
     const int half_w = H.wmax >> 1;
     __syncthreads();  // every thread has finished reading the transform buffers
 #pragma unroll
     for (int e = 0; e < 16; e++) {
         const int i2 = t + e * T - H.hw0;
-        if (i2 >= 0 && i2 < half_w) {
-#pragma unroll
-            for (int nb = 0; nb < NB; nb++)
-                pw[2 * i2 + (SPLIT ? half : nb)] = fmaf(x[nb][e].x, x[nb][e].x, x[nb][e].y * x[nb][e].y);
-        }
+        if (i2 >= 0 && i2 < half_w) *reinterpret_cast<float2*>(pw + 2 * i2) = p[e];
     }
     __syncthreads();
     return pw;
@@ -154,7 +152,6 @@ template <int M, bool F16, bool SPLIT>
 __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLIT, M>::MINB)
     k_plane(const PlaneArgs a, const float2* __restrict__ tw) {
     constexpr int T = M / 16;
-    constexpr int NB = PlaneShape<SPLIT, M>::NB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // segments vary fastest across the grid, so that the CTAs resident at
     // one time share a few templates (read from DRAM once, then from L2)
@@ -165,26 +162,35 @@ __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLI
     const HarmPlan& H = a.h[hi];
     const int z = item - H.zbase;
     const int seg = blockIdx.x;
-    const int half = SPLIT ? (int)(threadIdx.x / T) : 0;
-    const int t = SPLIT ? (int)(threadIdx.x % T) : (int)threadIdx.x;
-    float2 x[NB][16];
-    plane_transform<M, F16, SPLIT>(H, a.dbuf + (long long)seg * a.dstride + H.doff, z,
-                                   reinterpret_cast<float2*>(smem_raw), tw, x, t, half);
-    // straight from registers: even/odd pairs as 8-byte stores (one thread
-    // holds both), or single floats interleaved by the two halves
+    const int t = threadIdx.x;
+    const float2* __restrict__ D = a.dbuf + (long long)seg * a.dstride + H.doff;
     float* row = a.planes + (long long)seg * a.pstride + H.poff + (long long)z * H.prow;
     const int half_w = H.wmax >> 1;
+    if constexpr (!SPLIT) {
+        // straight from registers: (even, odd) pairs as 8-byte stores
+        float2 p[16];
+        plane_powers<M, F16, false>(H, D, z, reinterpret_cast<float2*>(smem_raw), tw, p, t);
 #pragma unroll
-    for (int e = 0; e < 16; e++) {
-        const int i2 = t + e * T - H.hw0;
-        if (i2 >= 0 && i2 < half_w) {
-            if constexpr (NB == 2) {
-                float2 p;
-                p.x = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y);
-                p.y = fmaf(x[1][e].x, x[1][e].x, x[1][e].y * x[1][e].y);
-                *reinterpret_cast<float2*>(row + 2 * i2) = p;
-            } else {
-                row[2 * i2 + half] = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y);
+        for (int e = 0; e < 16; e++) {
+            const int i2 = t + e * T - H.hw0;
+            if (i2 >= 0 && i2 < half_w) *reinterpret_cast<float2*>(row + 2 * i2) = p[e];
+        }
+    } else {
+        // even transform, then odd, each stored as it completes (a loop, not
+        // unrolled, so that nothing of the first stays live in the second)
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {
+            float2 x[1][16];
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+                const int idx = t + e * T;
+                x[0][e] = cmul(D[idx], fold_at<M, F16>(H, z, half, idx));
+            }
+            fft_run<M, +1, 1>(x, reinterpret_cast<float2*>(smem_raw), tw, t);
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+                const int i2 = t + e * T - H.hw0;
+                if (i2 >= 0 && i2 < half_w) row[2 * i2 + half] = fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y);
             }
         }
     }
@@ -232,21 +238,18 @@ __device__ __forceinline__ void append_candidates(bool hit, int seg, int i, int 
     }
 }
 
-template <int M, bool F16, bool SPLIT>
-__global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLIT, M>::MINB)
+template <int M, bool F16>
+__global__ void __launch_bounds__(PlaneShape<false, M>::THREADS, PlaneShape<false, M>::MINB)
     k_fund_sum(const FundArgs a, const float2* __restrict__ tw) {
-    constexpr int T = M / 16;
-    constexpr int THREADS = PlaneShape<SPLIT, M>::THREADS;
+    constexpr int THREADS = PlaneShape<false, M>::THREADS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const HarmPlan& H0 = a.h[0];
     const int z = blockIdx.x;
     const int seg = blockIdx.y;
-    const int half = SPLIT ? (int)(threadIdx.x / T) : 0;
-    const int t = SPLIT ? (int)(threadIdx.x % T) : (int)threadIdx.x;
-    float2 x[PlaneShape<SPLIT, M>::NB][16];
-    plane_transform<M, F16, SPLIT>(H0, a.dbuf + (long long)seg * a.dstride + H0.doff, z,
-                                   reinterpret_cast<float2*>(smem_raw), tw, x, t, half);
-    const float* pw = stage_row_powers<M, SPLIT>(H0, smem_raw, x, t, half);
+    float2 p[16];
+    plane_powers<M, F16, false>(H0, a.dbuf + (long long)seg * a.dstride + H0.doff, z,
+                                reinterpret_cast<float2*>(smem_raw), tw, p, (int)threadIdx.x);
+    const float* pw = stage_row_powers<M>(H0, smem_raw, p, (int)threadIdx.x);
 
     const long long startr = a.segs[seg].startr;
     const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
@@ -527,7 +530,7 @@ template <int M> static int prep_m(const PrepArgs& a, int nseg, const float2* tw
 
 template <int M, bool F16, bool SPLIT>
 static int plane_m(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st) {
-    size_t smem = sizeof(float2) * FftShape<M>::PADDED * 2;
+    size_t smem = sizeof(float2) * FftShape<M>::PADDED * PlaneShape<SPLIT, M>::BUFFERS;
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -548,27 +551,27 @@ static int plane_dispatch(const PlaneArgs& a, int nseg, const float2* tw, cudaSt
     return sp ? plane_m<M, false, true>(a, nseg, tw, st) : plane_m<M, false, false>(a, nseg, tw, st);
 }
 
-template <int M, bool F16, bool SPLIT>
+template <int M, bool F16>
 static int fund_m(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st) {
     size_t smem = sizeof(float2) * FftShape<M>::PADDED * 2;
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_fund_sum<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess ||
-            cudaFuncSetAttribute(k_fund_sum<M, F16, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
         attr = true;
     }
-    k_fund_sum<M, F16, SPLIT><<<dim3(a.h[0].numzs, nseg), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
+    k_fund_sum<M, F16><<<dim3(a.h[0].numzs, nseg), PlaneShape<false, M>::THREADS, smem, st>>>(a, tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// The fused kernel always uses the two-transform layout (it stages the
+// row's powers in shared memory, which the sequential layout keeps busy).
 template <int M>
 static int fund_dispatch(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st) {
-    const bool h = a.use_fp16 != 0, sp = a.split != 0;
-    if (h) return sp ? fund_m<M, true, true>(a, nseg, tw, st) : fund_m<M, true, false>(a, nseg, tw, st);
-    return sp ? fund_m<M, false, true>(a, nseg, tw, st) : fund_m<M, false, false>(a, nseg, tw, st);
+    return a.use_fp16 ? fund_m<M, true>(a, nseg, tw, st) : fund_m<M, false>(a, nseg, tw, st);
 }
 
 }  // namespace accel

@@ -91,7 +91,9 @@ typedef struct accel_stats {
 typedef struct accel_tuning {
     int chunk_segments;     /* overlap-save steps per launch group            */
     int plane_split;        /* plane kernel: 0 one thread carries the even and */
-                            /* the odd transform, 1 separate threads          */
+                            /* the odd transform at once, 1 it runs them one  */
+                            /* after the other (fewer registers, more CTAs    */
+                            /* per SM); the fused sum always uses 0           */
     int fused_sum;          /* 1: sum harmonics inside the fundamental's plane */
                             /* kernel; 0: store all planes, tiled sum kernel  */
     int hsum_rowwise;       /* 1: row-wise harmonic-sum kernel instead of the  */
