@@ -99,6 +99,7 @@ struct HsumArgs {
     int seg_base;           // added to the segment index stored in candidates
     float* stage_out;       // optional [nseg][nstages][numzs0][uselen]
     int nstages;
+    unsigned long long* err;  // bit 0: a tile's copy wait timed out
 };
 
 // Fundamental plane fused with the harmonic sum (k_fund_sum).

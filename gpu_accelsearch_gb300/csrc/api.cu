@@ -356,8 +356,9 @@ int alloc_work(accel_ctx* c) {
     }
     c->cand_cap = c->cfg.cand_capacity > 0 ? c->cfg.cand_capacity : (1LL << 22);
     CK(cudaMalloc(&c->d_cands, sizeof(RawCand) * c->cand_cap));
-    CK(cudaMalloc(&c->d_ncand, sizeof(unsigned long long)));
-    CK(cudaMallocHost(&c->h_ncand, sizeof(unsigned long long)));
+    // [0] candidate count, [1] kernel error bits
+    CK(cudaMalloc(&c->d_ncand, 2 * sizeof(unsigned long long)));
+    CK(cudaMallocHost(&c->h_ncand, 2 * sizeof(unsigned long long)));
     return ACCEL_OK;
 }
 
@@ -536,6 +537,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ha.seg_base = seg_base;
         ha.stage_out = stage_out;
         ha.nstages = c->nstages;
+        ha.err = c->d_ncand + 1;
         ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
@@ -575,7 +577,7 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
             d.trial = i;
             d.step = (int)s;
         }
-    CK(cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), c->stream));
     if (total > 0)
         CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
                            c->stream));
@@ -611,9 +613,12 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         CK(cudaEventRecord(c->ev_fork, c->stream2));
         CK(cudaStreamWaitEvent(c->stream, c->ev_fork, 0));
     }
-    CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+    CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (c->h_ncand[1])
+        return set_err(ACCEL_ERR_CUDA, "harmonic sum: a tile's copy wait timed out (error bits %llx)",
+                       c->h_ncand[1]);
     unsigned long long nraw = *c->h_ncand;
     c->last_raw = nraw;
     long long keep = (long long)std::min<unsigned long long>(nraw, (unsigned long long)c->cand_cap);
@@ -1082,11 +1087,14 @@ int accel_sum_harmonics(accel_ctx* c, const float* planes, const long long* star
         return set_err(ACCEL_ERR_INVALID, "planes must be 16-byte aligned");
     int rc = ensure_device(c);
     if (!rc) rc = stage_segs(c, nullptr, 0, startr, nseg);
-    if (!rc) CK(cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), c->stream));
+    if (!rc) CK(cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), c->stream));
     if (!rc) rc = run_group(c, c->d_segs, nseg, 0, stage_out, nullptr, const_cast<float*>(planes), false, false, true);
     if (!rc) {
-        CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           c->stream));
         CK(cudaStreamSynchronize(c->stream));
+        if (c->h_ncand[1])
+            return set_err(ACCEL_ERR_CUDA, "harmonic sum: a tile's copy wait timed out");
         if (ncand) *ncand = (long long)*c->h_ncand;
     }
     return rc;

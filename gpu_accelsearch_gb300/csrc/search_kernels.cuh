@@ -300,19 +300,49 @@ __global__ void __launch_bounds__(PlaneShape<false, M>::THREADS, PlaneShape<fals
 // Harmonic sum of one tile of kTileZ f-dot rows x kTileI columns of the
 // fundamental plane.  The fundamental tile and, for every sub-harmonic, the
 // rectangle of its plane that the tile's (zind, rind) indices touch are
-// copied into shared memory first (16-byte cp.async, each element once per
-// tile), then every cell is summed from shared memory in the reference's
-// harmonic order and checked against the stage cuts.
+// brought into shared memory by bulk asynchronous copies (cp.async.bulk,
+// one per rectangle row, completing on one mbarrier), then every cell is
+// summed from shared memory in the reference's harmonic order and checked
+// against the stage cuts.
 constexpr int kTileZ = kHsumTileZ;
 constexpr int kTileI = kHsumTileI;
 constexpr int kTileSmemFloats = kHsumTileFloats;   // 60 KB: fundamental tile + sub-tiles
 
-__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Poll the barrier's phase; false after about 2^20 polls (tens of
+// milliseconds), far beyond any copy of a tile.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+#pragma unroll 1
+    for (int it = 0; it < (1 << 20); it++) {
+        if (mbar_test(bar, parity)) return true;
+        if (it >= 32) __nanosleep(32);
+    }
+    return false;
+}
+// bytes (a multiple of 16) from global to shared, both 16-byte aligned
+__device__ __forceinline__ void bulk_copy_g2s(void* sdst, const void* gsrc, unsigned bytes,
+                                              unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_addr(sdst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
 }
 
 // Stage index after harmonic h (bank order): stages end after 1, 2, 4, 8,
@@ -323,10 +353,12 @@ __host__ __device__ constexpr int stage_after(int h) {
 
 template <int NH, bool STAGE_OUT>
 __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
-    extern __shared__ __align__(16) float tsm[];
+    static_assert(NH <= 32, "one lane per harmonic");
+    extern __shared__ __align__(128) float tsm[];
     __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
-    __shared__ int s_zf[NH], s_nzr[NH], s_c0[NH], s_w4[NH], s_off[NH];
+    __shared__ int s_zf[NH], s_nzr[NH], s_r0[NH], s_c0[NH], s_w4[NH], s_off[NH];
     __shared__ long long s_rlo2[NH];
+    __shared__ __align__(8) unsigned long long s_bar;
     const int seg = blockIdx.z;
     const int z0 = blockIdx.y * kTileZ;
     const int i0 = blockIdx.x * kTileI;
@@ -338,11 +370,11 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     const int i = i0 + tid;
     const bool valid = tid < ni;
 
-    // 1. rectangles, lane h of warp 0 for harmonic h: rows [zf, zf + nzr),
-    //    4-aligned columns [c0, c0 + 4 w4), placed one after another in
-    //    shared memory (offsets by a warp prefix sum)
+    // 1. warp 0: rectangles, lane h for harmonic h -- rows [zf, zf + nzr),
+    //    4-aligned columns [c0, c0 + 4 w4) -- placed one after another in
+    //    shared memory (warp prefix sums), then one bulk copy per row
     if (tid < 32) {
-        int size = 0;
+        int size = 0, nzr = 0;
         if (tid < NH) {
             const int h = tid;
             const HarmPlan& H = a.h[h];
@@ -357,37 +389,56 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
             }
             const int c0 = rfirst & ~3;
             const int w4 = ((rlast - c0) >> 2) + 1;
+            nzr = zl - zf + 1;
             s_zf[h] = zf;
-            s_nzr[h] = zl - zf + 1;
+            s_nzr[h] = nzr;
             s_c0[h] = c0;
             s_w4[h] = w4;
             s_rlo2[h] = rlo2;
-            size = 4 * (zl - zf + 1) * w4;
+            size = 4 * nzr * w4;
         }
-        int incl = size;
+        int incl = size, rincl = nzr;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (tid >= o) incl += v;
+            const int w = __shfl_up_sync(0xffffffffu, rincl, o);
+            if (tid >= o) {
+                incl += v;
+                rincl += w;
+            }
         }
-        if (tid < NH) s_off[tid] = incl - size;
+        if (tid < NH) {
+            s_off[tid] = incl - size;
+            s_r0[tid] = rincl - nzr;  // first copy index of harmonic tid
+        }
+        const int total_floats = __shfl_sync(0xffffffffu, incl, 31);
+        const int total_rows = __shfl_sync(0xffffffffu, rincl, 31);
+        if (tid == 0) {
+            mbar_init(&s_bar, 1);
+            mbar_arrive_expect_tx(&s_bar, 4u * (unsigned)total_floats);
+        }
+        __syncwarp();
+        for (int j = tid; j < total_rows; j += 32) {
+            int h = 0;
+#pragma unroll
+            for (int g = 1; g < NH; g++)
+                if (j >= s_r0[g]) h = g;
+            const HarmPlan& H = a.h[h];
+            const int r = j - s_r0[h], w4 = s_w4[h];
+            bulk_copy_g2s(tsm + s_off[h] + 4 * w4 * r, P + H.poff + (long long)(s_zf[h] + r) * H.prow + s_c0[h],
+                          16u * (unsigned)w4, &s_bar);
+        }
     }
     __syncthreads();
-    // 2. copies (warps over rows, lanes over 16-byte chunks) and row table
+    // 2. row table and this thread's column in every rectangle (while the
+    //    copies fly)
 #pragma unroll
     for (int h = 0; h < NH; h++) {
-        const HarmPlan& H = a.h[h];
-        const int zf = s_zf[h], w4 = s_w4[h], off = s_off[h], nzr = s_nzr[h];
         if (tid < nz) {
-            const int r = (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), H) - zf;
-            s_row[h][tid] = off + 4 * w4 * r;
+            const int r = (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - s_zf[h];
+            s_row[h][tid] = s_off[h] + 4 * s_w4[h] * r;
         }
-        const float* src = P + H.poff + (long long)zf * H.prow + s_c0[h];
-        for (int r = tid >> 5; r < nzr; r += kTileI / 32)
-            for (int c = tid & 31; c < w4; c += 32)
-                cp_async16(tsm + off + 4 * (r * w4 + c), src + (long long)r * H.prow + 4 * c);
     }
-    // 3. this thread's column in every rectangle
     int col[NH];
 #pragma unroll
     for (int h = 0; h < NH; h++) {
@@ -403,8 +454,13 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
     float cut[kMaxStages];
 #pragma unroll
     for (int st = 0; st < kMaxStages; st++) cut[st] = a.cut[st];
-    cp_async_wait_all();
-    __syncthreads();
+    // 3. wait for the copies (bounded; every thread agrees on the outcome)
+    const bool landed = mbar_wait_bounded(&s_bar, 0);
+    if (!__syncthreads_and(landed)) {
+        if (tid == 0) atomicOr(a.err, 1ull);
+        mbar_wait_bounded(&s_bar, 0);  // give copies still in flight a last chance to land
+        return;
+    }
 
     // 4. sums in the reference's harmonic order; one warp vote over all
     //    stage tests, the per-stage appends only when some lane hit

@@ -171,17 +171,19 @@ bool run_one_group(accel_server* s, int zmax) {
     if (n == 0) return false;
     int rc = ACCEL_OK;
     if (cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * n, cudaMemcpyHostToDevice, s->stream) ||
-        cudaMemsetAsync(c->d_ncand, 0, sizeof(unsigned long long), s->stream))
+        cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), s->stream))
         rc = set_error(ACCEL_ERR_CUDA, "server: group upload");
     cudaEventRecord(s->ev0, s->stream);
     if (!rc) rc = run_group(c, c->d_segs, n, 0, nullptr, nullptr, nullptr, true, true, true, c->fused_sum != 0);
     cudaEventRecord(s->ev1, s->stream);
     std::vector<RawCand> raw;
     if (!rc) {
-        if (cudaMemcpyAsync(c->h_ncand, c->d_ncand, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        if (cudaMemcpyAsync(c->h_ncand, c->d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             s->stream) != cudaSuccess ||
             cudaStreamSynchronize(s->stream) != cudaSuccess)
             rc = set_error(ACCEL_ERR_CUDA, "server: group");
+        else if (c->h_ncand[1])
+            rc = set_error(ACCEL_ERR_CUDA, "server: a harmonic-sum tile's copy wait timed out");
     }
     if (!rc) {
         const long long nr = (long long)std::min<unsigned long long>(*c->h_ncand, (unsigned long long)c->cand_cap);
