@@ -317,23 +317,22 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, u
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+// Wait for the barrier's phase with the thread suspended (no polling
+// instructions), at most about 1 us per try; false after 2^15 tries (tens
+// of milliseconds), far beyond any copy of a tile.
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
     unsigned done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(1000u)
         : "memory");
     return done != 0;
 }
-// Poll the barrier's phase; false after about 2^20 polls (tens of
-// milliseconds), far beyond any copy of a tile.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
 #pragma unroll 1
-    for (int it = 0; it < (1 << 20); it++) {
-        if (mbar_test(bar, parity)) return true;
-        if (it >= 32) __nanosleep(32);
-    }
+    for (int it = 0; it < (1 << 15); it++)
+        if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 // bytes (a multiple of 16) from global to shared, both 16-byte aligned
@@ -352,12 +351,12 @@ __host__ __device__ constexpr int stage_after(int h) {
 }
 
 template <int NH, bool STAGE_OUT>
-__global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
+__global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
     static_assert(NH <= 32, "one lane per harmonic");
     extern __shared__ __align__(128) float tsm[];
     __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
     __shared__ int s_zf[NH], s_nzr[NH], s_r0[NH], s_c0[NH], s_w4[NH], s_off[NH];
-    __shared__ long long s_rlo2[NH];
+    __shared__ int s_cb[NH], s_crem[NH];  // column of tile column 0, and the rounding remainder
     __shared__ __align__(8) unsigned long long s_bar;
     const int seg = blockIdx.z;
     const int z0 = blockIdx.y * kTileZ;
@@ -394,8 +393,14 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
             s_nzr[h] = nzr;
             s_c0[h] = c0;
             s_w4[h] = w4;
-            s_rlo2[h] = rlo2;
             size = 4 * nzr * w4;
+            // twice_r_shift(2 startr + i0 + k) = (B + 2 k p) >> (lq + 1) with
+            // B = 2 (2 startr + i0) p + 2^lq: split B once so that every
+            // thread finishes in 32 bits (only the low 16 bits of the
+            // difference to rlo2 matter, as in the reference's ushort)
+            const long long B = 2LL * (2 * startr + i0) * H.p + (1LL << H.lq);
+            s_cb[h] = (int)((B >> (H.lq + 1)) - rlo2) - c0;
+            s_crem[h] = (int)(B & ((2LL << H.lq) - 1));
         }
         int incl = size, rincl = nzr;
 #pragma unroll
@@ -446,9 +451,9 @@ __global__ void __launch_bounds__(kTileI) k_hsum_tile(const HsumArgs a) {
             col[h] = tid;
         } else {
             const HarmPlan& H = a.h[h];
-            const int rind = valid ? (int)(unsigned short)(twice_r_shift(2 * startr + i, H.p, H.lq) - s_rlo2[h])
-                                   : s_c0[h];
-            col[h] = rind - s_c0[h];
+            const int c0 = s_c0[h];
+            const int rind = (unsigned short)(s_cb[h] + c0 + ((s_crem[h] + 2 * tid * H.p) >> (H.lq + 1)));
+            col[h] = valid ? rind - c0 : 0;
         }
     }
     float cut[kMaxStages];
