@@ -354,7 +354,7 @@ template <int NH, bool STAGE_OUT>
 __global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
     static_assert(NH <= 32, "one lane per harmonic");
     extern __shared__ __align__(128) float tsm[];
-    __shared__ int s_row[NH][kTileZ];  // shared-memory offset of the row used by tile row zr
+    __shared__ __align__(16) int s_row[NH][kTileZ];  // byte offset of the row used by tile row zr
     __shared__ int s_zf[NH], s_nzr[NH], s_r0[NH], s_c0[NH], s_w4[NH], s_off[NH];
     __shared__ int s_cb[NH], s_crem[NH];  // column of tile column 0, and the rounding remainder
     __shared__ __align__(8) unsigned long long s_bar;
@@ -437,23 +437,24 @@ __global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
     __syncthreads();
     // 2. row table and this thread's column in every rectangle (while the
     //    copies fly)
+    //    (rows past the plane's edge point at the rectangle's first row)
 #pragma unroll
     for (int h = 0; h < NH; h++) {
-        if (tid < nz) {
-            const int r = (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - s_zf[h];
-            s_row[h][tid] = s_off[h] + 4 * s_w4[h] * r;
+        if (tid < kTileZ) {
+            const int r = (tid >= nz) ? 0 : (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - s_zf[h];
+            s_row[h][tid] = 4 * (s_off[h] + 4 * s_w4[h] * r);
         }
     }
-    int col[NH];
+    int colb[NH];  // byte offset of this thread's column
 #pragma unroll
     for (int h = 0; h < NH; h++) {
         if (h == 0) {
-            col[h] = tid;
+            colb[h] = 4 * tid;
         } else {
             const HarmPlan& H = a.h[h];
             const int c0 = s_c0[h];
             const int rind = (unsigned short)(s_cb[h] + c0 + ((s_crem[h] + 2 * tid * H.p) >> (H.lq + 1)));
-            col[h] = valid ? rind - c0 : 0;
+            colb[h] = valid ? 4 * (rind - c0) : 0;
         }
     }
     float cut[kMaxStages];
@@ -467,34 +468,58 @@ __global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
         return;
     }
 
-    // 4. sums in the reference's harmonic order; one warp vote over all
-    //    stage tests, the per-stage appends only when some lane hit
-#pragma unroll 2
-    for (int zr = 0; zr < nz; zr++) {
-        const int z = z0 + zr;
-        float s = 0.f, sst[kMaxStages];
-        bool any = false;
+    // 4. sums in the reference's harmonic order, RB rows at a time (their
+    //    row offsets in one vector load per harmonic); one warp vote per
+    //    row over all stage tests, the per-stage appends only when some
+    //    lane hit
+    constexpr int RB = (NH <= 8 && !STAGE_OUT) ? 4 : 2;  // rows per batch (registers)
+    const char* tb = reinterpret_cast<const char*>(tsm);
+#pragma unroll 1
+    for (int zq = 0; zq < nz; zq += RB) {
+        int ro[NH][RB];
 #pragma unroll
         for (int h = 0; h < NH; h++) {
-            const float v = tsm[s_row[h][zr] + col[h]];
-            s = (h == 0) ? v : s + v;
-            const int st = stage_after(h);  // folds to a constant once h is unrolled
-            if (st >= 0) {
-                sst[st] = s;
-                any |= s > cut[st];
-                if constexpr (STAGE_OUT) {
-                    if (valid)
-                        a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
-                }
+            if constexpr (RB == 4) {
+                const int4 v = *reinterpret_cast<const int4*>(&s_row[h][zq]);
+                ro[h][0] = v.x;
+                ro[h][1] = v.y;
+                ro[h][2] = v.z;
+                ro[h][3] = v.w;
+            } else {
+                const int2 v = *reinterpret_cast<const int2*>(&s_row[h][zq]);
+                ro[h][0] = v.x;
+                ro[h][1] = v.y;
             }
         }
-        if (__any_sync(0xffffffffu, valid && any)) {
+#pragma unroll
+        for (int k = 0; k < RB; k++) {
+            const int zr = zq + k;
+            const int z = z0 + zr;
+            const bool live = valid && zr < nz;
+            float s = 0.f, sst[kMaxStages];
+            bool any = false;
 #pragma unroll
             for (int h = 0; h < NH; h++) {
-                const int st = stage_after(h);
-                if (st >= 0)
-                    append_candidates(valid && sst[st] > cut[st], a.seg_base + seg, i, z, h + 1, sst[st],
-                                      a.cands, a.ncand, a.cap);
+                const float v = *reinterpret_cast<const float*>(tb + ro[h][k] + colb[h]);
+                s = (h == 0) ? v : s + v;
+                const int st = stage_after(h);  // folds to a constant once h is unrolled
+                if (st >= 0) {
+                    sst[st] = s;
+                    any |= s > cut[st];
+                    if constexpr (STAGE_OUT) {
+                        if (live)
+                            a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] = s;
+                    }
+                }
+            }
+            if (__any_sync(0xffffffffu, live && any)) {
+#pragma unroll
+                for (int h = 0; h < NH; h++) {
+                    const int st = stage_after(h);
+                    if (st >= 0)
+                        append_candidates(live && sst[st] > cut[st], a.seg_base + seg, i, z, h + 1, sst[st],
+                                          a.cands, a.ncand, a.cap);
+                }
             }
         }
     }
