@@ -134,6 +134,7 @@ int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
 int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st);
+int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st);
 // Tile geometry of launch_hsum_tile (the host proves the shared-memory bound).
 constexpr int kHsumTileZ = 16;
 constexpr int kHsumTileI = 256;

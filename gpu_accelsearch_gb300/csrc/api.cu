@@ -541,7 +541,9 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
-        if (c->tile_ok && c->hsum_tiled)
+        if (c->tile_ok && c->hsum_tiled && c->hsum_pipe)
+            CKL(launch_hsum_pipe(ha, nseg, sum_stream), "harmonic sum (tiled, pipelined)");
+        else if (c->tile_ok && c->hsum_tiled)
             CKL(launch_hsum_tile(ha, nseg, sum_stream), "harmonic sum (tiled)");
         else
             CKL(launch_hsum(ha, nseg, sum_stream), "harmonic sum");
@@ -844,6 +846,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->fused_sum = c->fused_sum;
     t->hsum_rowwise = !c->hsum_tiled;
     t->serial_sum = !c->overlap;
+    t->hsum_pipelined = c->hsum_pipe;
     return ACCEL_OK;
 }
 
@@ -857,6 +860,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->fused_sum = t->fused_sum != 0;
     c->hsum_tiled = t->hsum_rowwise == 0;
     c->overlap = t->serial_sum == 0;
+    c->hsum_pipe = t->hsum_pipelined != 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaStreamSynchronize(c->stream2));

@@ -63,6 +63,7 @@ struct accel_ctx {
     cudaEvent_t ev_fork = nullptr, ev_plane[2] = {nullptr, nullptr}, ev_sum[2] = {nullptr, nullptr};
     bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
     int hsum_tiled = 1;
+    int hsum_pipe = 0;      // persistent pipelined tile kernel
     int tile_floats = 0;
     float2* dbuf = nullptr;
     float* planes = nullptr;

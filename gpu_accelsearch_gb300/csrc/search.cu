@@ -1,6 +1,8 @@
 // search.cu -- kernel instantiations (segment preparation and harmonic sum; dispatch).
 #include "search_kernels.cuh"
 
+#include <algorithm>
+
 namespace accel {
 
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st) {
@@ -43,6 +45,42 @@ static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t 
     }
     k_hsum_tile<NH, SO><<<grid, kTileI, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NH, bool SO>
+static int hsum_pipe_nh(const HsumArgs& a, int ntiles, cudaStream_t st) {
+    static bool attr = false;
+    const size_t smem = sizeof(float) * kTileSmemFloats * kPipeBufs;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return -1;
+    const int grid = std::max(1, std::min(ntiles, sms));
+    k_hsum_pipe<NH, SO><<<grid, kPipeThreads, smem, st>>>(a, ntiles);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st) {
+    const long long nt = (long long)((a.uselen + kTileI - 1) / kTileI) * ((a.numzs0 + kTileZ - 1) / kTileZ) * nseg;
+    if (nt >= (1LL << 31)) return -1;
+    const int ntiles = (int)nt;
+    const bool so = a.stage_out != nullptr;
+    switch (a.nh) {
+        case 1: return so ? hsum_pipe_nh<1, true>(a, ntiles, st) : hsum_pipe_nh<1, false>(a, ntiles, st);
+        case 2: return so ? hsum_pipe_nh<2, true>(a, ntiles, st) : hsum_pipe_nh<2, false>(a, ntiles, st);
+        case 4: return so ? hsum_pipe_nh<4, true>(a, ntiles, st) : hsum_pipe_nh<4, false>(a, ntiles, st);
+        case 8: return so ? hsum_pipe_nh<8, true>(a, ntiles, st) : hsum_pipe_nh<8, false>(a, ntiles, st);
+        case 16: return so ? hsum_pipe_nh<16, true>(a, ntiles, st) : hsum_pipe_nh<16, false>(a, ntiles, st);
+    }
+    return -1;
 }
 
 int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st) {

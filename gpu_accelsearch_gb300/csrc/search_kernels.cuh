@@ -313,6 +313,9 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned coun
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
@@ -519,6 +522,212 @@ __global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
                     if (st >= 0)
                         append_candidates(live && sst[st] > cut[st], a.seg_base + seg, i, z, h + 1, sst[st],
                                           a.cands, a.ncand, a.cap);
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------- pipelined tiled hsum
+// The same tiles and sums as k_hsum_tile, from one persistent CTA per SM
+// with kPipeBufs tile buffers in shared memory and specialised warps: one
+// producer warp computes each tile's rectangles and issues its bulk copies
+// (completing on the buffer's "full" mbarrier) as soon as the consumers
+// have released the buffer (its "empty" mbarrier); 16 consumer warps, two
+// threads per column and 8 rows each, sum the tiles in order.  DRAM reads
+// of the next tiles overlap the additions of the current one.  Every wait
+// is bounded; a warp that gives up sets the error word, lets the copies it
+// knows of land, and leaves.
+constexpr int kPipeBufs = 3;
+constexpr int kPipeConsumers = 2 * kTileI;                 // 512 threads, 16 warps
+constexpr int kPipeThreads = kPipeConsumers + 32 * kPipeBufs;  // + one producer warp per buffer
+
+template <int NH, bool STAGE_OUT>
+__global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a, int ntiles) {
+    static_assert(NH <= 32, "one lane per harmonic");
+    static_assert(kTileZ == 16 && kTileI == 256, "two threads per column, 8 rows each");
+    extern __shared__ __align__(128) float tsm[];  // kPipeBufs x kTileSmemFloats
+    __shared__ __align__(16) int s_row[kPipeBufs][NH][kTileZ];  // byte offset of tile row zr's row
+    __shared__ int s_c0[kPipeBufs][NH], s_cb[kPipeBufs][NH], s_crem[kPipeBufs][NH];
+    __shared__ int s_tile[kPipeBufs][4];  // seg, z0, i0, nz | ni << 16
+    __shared__ __align__(8) unsigned long long s_full[kPipeBufs], s_empty[kPipeBufs];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int G = gridDim.x;
+    if (tid == 0)
+        for (int b = 0; b < kPipeBufs; b++) {
+            mbar_init(&s_full[b], 1);
+            mbar_init(&s_empty[b], kPipeConsumers / 32);
+        }
+    __syncthreads();
+
+    if (tid >= kPipeConsumers) {
+        // ------------------------------------------------------ producers
+        // producer warp b owns buffer b and fills it with tiles k = b,
+        // b + kPipeBufs, ... of this CTA
+        const int b = (tid - kPipeConsumers) >> 5;
+        const int ntz = (a.numzs0 + kTileZ - 1) / kTileZ;
+        const int nti = (a.uselen + kTileI - 1) / kTileI;
+#pragma unroll 1
+        for (int k = b; blockIdx.x + (long long)k * G < ntiles; k += kPipeBufs) {
+            const int t = blockIdx.x + k * G;
+            const unsigned use = (unsigned)(k / kPipeBufs);  // how often b was filled before
+            if (use > 0 && !mbar_wait_bounded(&s_empty[b], (use - 1) & 1u)) {
+                if (lane == 0) atomicOr(a.err, 1ull);
+                mbar_wait_bounded(&s_full[b], (use - 1) & 1u);  // let the previous fill's copies land
+                return;
+            }
+            const int it = t % nti, rest = t / nti;
+            const int zt = rest % ntz, seg = rest / ntz;
+            const int z0 = zt * kTileZ, i0 = it * kTileI;
+            const int nz = min(kTileZ, a.numzs0 - z0), ni = min(kTileI, a.uselen - i0);
+            const long long startr = a.segs[seg].startr;
+            int size = 0, nzr = 0, zf = z0, c0 = 0, w4 = 0;
+            if (lane < NH) {
+                const int h = lane;
+                const HarmPlan& H = a.h[h];
+                int rfirst = i0, rlast = i0 + ni - 1, zl = z0 + nz - 1;
+                long long rlo2 = 0;
+                if (h > 0) {
+                    rlo2 = (twice_r_shift(2 * startr, H.p, H.lq) >> 1) << 1;
+                    rfirst = (int)(unsigned short)(twice_r_shift(2 * startr + i0, H.p, H.lq) - rlo2);
+                    rlast = (int)(unsigned short)(twice_r_shift(2 * startr + i0 + ni - 1, H.p, H.lq) - rlo2);
+                    zf = sub_row(a.zlo0 + kDz * z0, H);
+                    zl = sub_row(a.zlo0 + kDz * (z0 + nz - 1), H);
+                }
+                c0 = rfirst & ~3;
+                w4 = ((rlast - c0) >> 2) + 1;
+                nzr = zl - zf + 1;
+                size = 4 * nzr * w4;
+                const long long B = 2LL * (2 * startr + i0) * H.p + (1LL << H.lq);
+                s_c0[b][h] = c0;
+                s_cb[b][h] = (int)((B >> (H.lq + 1)) - rlo2) - c0;
+                s_crem[b][h] = (int)(B & ((2LL << H.lq) - 1));
+            }
+            int incl = size;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int off = incl - size;
+            const int total_floats = __shfl_sync(0xffffffffu, incl, 31);
+            // row table: lane zr < 16 fills row zr of every harmonic (rows
+            // past the plane's edge use the rectangle's first row)
+#pragma unroll
+            for (int h = 0; h < NH; h++) {
+                const int offh = __shfl_sync(0xffffffffu, off, h), w4h = __shfl_sync(0xffffffffu, w4, h);
+                const int zfh = __shfl_sync(0xffffffffu, zf, h);
+                if (lane < kTileZ) {
+                    const int r = (lane >= nz) ? 0 : (h == 0) ? lane : sub_row(a.zlo0 + kDz * (z0 + lane), a.h[h]) - zfh;
+                    s_row[b][h][lane] = 4 * (offh + 4 * w4h * r);
+                }
+            }
+            if (lane == 0) {
+                s_tile[b][0] = seg;
+                s_tile[b][1] = z0;
+                s_tile[b][2] = i0;
+                s_tile[b][3] = nz | (ni << 16);
+            }
+            __syncwarp();  // the tables above are released by lane 0's arrive
+            if (lane == 0) mbar_arrive_expect_tx(&s_full[b], 4u * (unsigned)total_floats);
+            __syncwarp();
+            // copies: lane h brings rectangle h row by row
+            if (lane < NH) {
+                const HarmPlan& H = a.h[lane];
+                const float* src = a.planes + (long long)seg * a.pstride + H.poff + (long long)zf * H.prow + c0;
+                float* dst = tsm + b * kTileSmemFloats + off;
+                for (int r = 0; r < nzr; r++)
+                    bulk_copy_g2s(dst + 4 * w4 * r, src + (long long)r * H.prow, 16u * (unsigned)w4, &s_full[b]);
+            }
+        }
+        return;
+    }
+
+    // --------------------------------------------------------- consumers
+    const int c = tid & (kTileI - 1), rh = (tid / kTileI) * (kTileZ / 2);  // column, first row
+    constexpr int RB = (NH <= 8 && !STAGE_OUT) ? 4 : 2;                      // rows per batch
+    float cut[kMaxStages];
+#pragma unroll
+    for (int st = 0; st < kMaxStages; st++) cut[st] = a.cut[st];
+    int k = 0;
+#pragma unroll 1
+    for (int t = blockIdx.x; t < ntiles; t += G, k++) {
+        const int b = k % kPipeBufs;
+        const unsigned parity = (unsigned)(k / kPipeBufs) & 1u;
+        if (!mbar_wait_bounded(&s_full[b], parity)) {
+            if (lane == 0) atomicOr(a.err, 1ull);
+            mbar_wait_bounded(&s_full[b], parity);  // a last chance for the copies to land
+            return;
+        }
+        const int seg = s_tile[b][0], z0 = s_tile[b][1], i0 = s_tile[b][2];
+        const int nz = s_tile[b][3] & 0xffff, ni = s_tile[b][3] >> 16;
+        const int i = i0 + c;
+        const bool valid = c < ni;
+        int colb[NH];
+#pragma unroll
+        for (int h = 0; h < NH; h++) {
+            if (h == 0) {
+                colb[h] = 4 * c;
+            } else {
+                const HarmPlan& H = a.h[h];
+                const int c0 = s_c0[b][h];
+                const int rind = (unsigned short)(s_cb[b][h] + c0 + ((s_crem[b][h] + 2 * c * H.p) >> (H.lq + 1)));
+                colb[h] = valid ? 4 * (rind - c0) : 0;
+            }
+        }
+        const char* tb = reinterpret_cast<const char*>(tsm + b * kTileSmemFloats);
+        int ro[NH][kTileZ / 2];
+#pragma unroll
+        for (int h = 0; h < NH; h++)
+#pragma unroll
+            for (int q = 0; q < kTileZ / 2; q += 4) {
+                const int4 v = *reinterpret_cast<const int4*>(&s_row[b][h][rh + q]);
+                ro[h][q] = v.x;
+                ro[h][q + 1] = v.y;
+                ro[h][q + 2] = v.z;
+                ro[h][q + 3] = v.w;
+            }
+        float sums[kMaxStages][kTileZ / 2];
+        // all reads of buffer b done before it is released
+#pragma unroll
+        for (int zz = 0; zz < kTileZ / 2; zz++) {
+            float s = 0.f;
+#pragma unroll
+            for (int h = 0; h < NH; h++) {
+                const float v = *reinterpret_cast<const float*>(tb + ro[h][zz] + colb[h]);
+                s = (h == 0) ? v : s + v;
+                const int st = stage_after(h);  // folds to a constant once h is unrolled
+                if (st >= 0) sums[st][zz] = s;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&s_empty[b]);
+        if (rh < nz) {
+#pragma unroll
+            for (int zz = 0; zz < kTileZ / 2; zz++) {
+                const int zr = rh + zz;
+                const int z = z0 + zr;
+                const bool live = valid && zr < nz;
+                bool any = false;
+#pragma unroll
+                for (int st = 0; st < kMaxStages; st++) {
+                    if (st < stage_after(NH - 1) + 1) {
+                        any |= sums[st][zz] > cut[st];
+                        if constexpr (STAGE_OUT) {
+                            if (live)
+                                a.stage_out[(((long long)seg * a.nstages + st) * a.numzs0 + z) * a.uselen + i] =
+                                    sums[st][zz];
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, live && any)) {
+#pragma unroll
+                    for (int st = 0; st < kMaxStages; st++) {
+                        if (st < stage_after(NH - 1) + 1)
+                            append_candidates(live && sums[st][zz] > cut[st], a.seg_base + seg, i, z, 1 << st,
+                                              sums[st][zz], a.cands, a.ncand, a.cap);
+                    }
                 }
             }
         }

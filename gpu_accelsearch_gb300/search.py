@@ -148,10 +148,11 @@ class AccelSearch:
         N.check(N.lib().accel_get_tuning(self._h, C.byref(t)))
         return {"chunk_segments": t.chunk_segments, "plane_split": t.plane_split,
                 "fused_sum": t.fused_sum,
-                "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum}
+                "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum,
+                "hsum_pipelined": t.hsum_pipelined}
 
     def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
-                   hsum_rowwise=None, serial_sum=None):
+                   hsum_rowwise=None, serial_sum=None, hsum_pipelined=None):
         cur = self.tuning()
         t = N.Tuning()
         t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
@@ -159,6 +160,7 @@ class AccelSearch:
         t.fused_sum = cur["fused_sum"] if fused_sum is None else int(fused_sum)
         t.hsum_rowwise = cur["hsum_rowwise"] if hsum_rowwise is None else int(hsum_rowwise)
         t.serial_sum = cur["serial_sum"] if serial_sum is None else int(serial_sum)
+        t.hsum_pipelined = cur["hsum_pipelined"] if hsum_pipelined is None else int(hsum_pipelined)
         N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
 
     def profile(self, enable: bool = True):

@@ -100,7 +100,10 @@ typedef struct accel_tuning {
                             /* shared-memory tiled one                        */
     int serial_sum;         /* 1: no overlap of a group's harmonic sum (second */
                             /* stream) with the next group's transforms       */
-    int reserved[3];
+    int hsum_pipelined;     /* 1: tiled sum from persistent CTAs that overlap */
+                            /* the next tiles' copies with the current sums   */
+                            /* (producer warps); 0: one CTA per tile          */
+    int reserved[2];
 } accel_tuning;
 
 typedef struct accel_ctx accel_ctx;

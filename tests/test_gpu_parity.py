@@ -218,26 +218,26 @@ def test_batched_equals_single(S, trial):
                           np.sort(both, order=["trial", "step", "numharm", "z", "r"]))
 
 
-@pytest.mark.parametrize("split,fused,chunk,serial,rowwise",
-                         [(0, 1, 7, 0, 0), (1, 1, 64, 1, 0), (0, 0, 64, 1, 0), (1, 0, 1, 0, 0),
-                          (0, 0, 33, 0, 1), (1, 0, 5, 0, 0), (0, 0, 2, 0, 0)])
-def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwise):
+@pytest.mark.parametrize("split,fused,chunk,serial,rowwise,pipelined",
+                         [(0, 1, 7, 0, 0, 0), (1, 1, 64, 1, 0, 0), (0, 0, 64, 1, 0, 1), (1, 0, 1, 0, 0, 0),
+                          (0, 0, 33, 0, 1, 0), (1, 0, 5, 0, 0, 1), (0, 0, 2, 0, 0, 0), (0, 0, 3, 1, 0, 0)])
+def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwise, pipelined):
     # every launch shape gives bit-identical candidates (same float operations)
     w, rlo = trial["w"], trial["rlo"]
     d = dev(w)
     S.set_power_cuts(np.array([6.6, 9.2, 13.1], np.float32))  # ~3 sigma: many candidates
     try:
         S.set_tuning(chunk_segments=64, plane_split=0, fused_sum=0, serial_sum=1,
-                     hsum_rowwise=0)
+                     hsum_rowwise=0, hsum_pipelined=0)
         S.search_spectra([d.data_ptr()], [w.size], [rlo])
         base = S.candidates()
         S.set_tuning(chunk_segments=chunk, plane_split=split, fused_sum=fused,
-                     serial_sum=serial, hsum_rowwise=rowwise)
+                     serial_sum=serial, hsum_rowwise=rowwise, hsum_pipelined=pipelined)
         S.search_spectra([d.data_ptr()], [w.size], [rlo])
         got = S.candidates()
     finally:
         S.set_tuning(chunk_segments=64, plane_split=0, fused_sum=0, serial_sum=1,
-                     hsum_rowwise=0)
+                     hsum_rowwise=0, hsum_pipelined=0)
         S.set_power_cuts([O.power_cut(6.0, 1 << s) for s in range(S.nstages)])
     assert len(base) > 10000
     assert np.array_equal(base, got)
