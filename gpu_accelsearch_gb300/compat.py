@@ -37,6 +37,8 @@ SIGNATURES = {
     "accel_compat_get_uselen": (C.c_int, []),
     "accel_compat_status": (C.c_int, []),
     "createSubharmonicInfo": (C.POINTER(SubharmonicInfo), [C.c_int, C.c_int]),
+    "readData": (C.c_long, [C.c_char_p, C.POINTER(C.POINTER(C.c_float))]),
+    "freeData": (None, [C.POINTER(C.c_float)]),
     "freeSubharmonicInfo": (None, [C.POINTER(SubharmonicInfo), C.c_int]),
     "calc_required_z": (C.c_int, [C.c_double, C.c_double]),
     "calc_required_r": (C.c_double, [C.c_double, C.c_double]),

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -312,6 +313,57 @@ void freeSubharmonicInfo(SubharmonicInfo* shi, int nh) {
         cudaFree(shi[h].kernels_data);
     }
     std::free(shi);
+}
+
+// readData (bpd_data.c:9-75): the file's float32 samples behind
+// kDatPadding zero samples, with as many zeros after them; *output_data
+// points at the first sample.  The reference exits on a missing, empty or
+// longer-than-2^26-sample file; here it returns 0 with the status set.
+constexpr long kDatPadding = 2000;       // ACCEL_PADDING, bpd_common.h:35
+constexpr long kDatMaxSamples = 1L << 26;
+long readData(char* path, float** output_data) {
+    g_cs.status = ACCEL_OK;
+    if (!path || !output_data) {
+        fail(ACCEL_ERR_INVALID, "readData: null argument");
+        return 0;
+    }
+    *output_data = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        fail(ACCEL_ERR_INVALID, "readData: cannot open the file");
+        return 0;
+    }
+    long n = -1;
+    if (std::fseek(f, 0, SEEK_END) == 0) {
+        const long bytes = std::ftell(f);
+        if (bytes >= 0) n = bytes / (long)sizeof(float);
+    }
+    if (n <= 0 || n > kDatMaxSamples) {
+        std::fclose(f);
+        fail(ACCEL_ERR_INVALID, n <= 0 ? "readData: empty or unreadable file"
+                                       : "readData: the time series is longer than 2^26 samples");
+        return 0;
+    }
+    float* buf = (float*)std::calloc((size_t)(n + 2 * kDatPadding), sizeof(float));
+    if (!buf) {
+        std::fclose(f);
+        fail(ACCEL_ERR_NOMEM, "readData: host allocation");
+        return 0;
+    }
+    const bool ok = std::fseek(f, 0, SEEK_SET) == 0 &&
+                    std::fread(buf + kDatPadding, sizeof(float), (size_t)n, f) == (size_t)n;
+    std::fclose(f);
+    if (!ok) {
+        std::free(buf);
+        fail(ACCEL_ERR_INVALID, "readData: reading the file");
+        return 0;
+    }
+    *output_data = buf + kDatPadding;
+    return n;
+}
+
+void freeData(float* data) {
+    if (data) std::free(data - kDatPadding);
 }
 
 unsigned realToComplexFFT(float* idata, long n, accel_complex** odata, int batch) {

@@ -83,6 +83,14 @@ int    getTotalHarmonics(int harmonicStages);
  * this by hand, AccelSearch.cu:272-277). */
 void   freeSubharmonicInfo(SubharmonicInfo *shi, int totalHarmonics);
 
+/* bpd_data.h:13 (bpd_data.c:9-75): read a raw float32 time series (at most
+ * 2^26 samples); *output_data points at the first sample inside a buffer
+ * padded with 2000 zero samples on each side.  Returns the number of
+ * samples, or 0 with accel_compat_status() set (the reference exits).
+ * freeData releases the buffer (the reference never frees it). */
+long readData(char *path, float **output_data);
+void freeData(float *data);
+
 /* bpd_fft.cuh:14-16: realToComplexFFT takes host samples and returns a
  * malloc'd host spectrum of n/2+1 bins (caller frees), like the reference. */
 unsigned realToComplexFFT(float *idata, long inputElements, accel_complex **odata, int batch);

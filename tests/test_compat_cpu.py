@@ -81,3 +81,28 @@ def test_required_and_indices(L, pins):
         assert got == want
     assert L.getTotalHarmonics(4) == 8
     assert L.index_from_r(20000.5, 20000.0) == 1 and L.index_from_z(-48.0, -50.0) == 1
+
+
+def test_read_data_padding_and_limits(L, tmp_path):
+    # readData (bpd_data.c:9-75): samples behind 2000 zero samples, 2000 zeros
+    # after them, at most 2^26 samples; errors come back as a status
+    x = np.random.default_rng(5).standard_normal(12345).astype(np.float32)
+    f = tmp_path / "series.dat"
+    x.tofile(f)
+    p = C.POINTER(C.c_float)()
+    n = L.readData(str(f).encode(), C.byref(p))
+    assert L.accel_compat_status() == 0 and n == x.size
+    base = C.cast(C.addressof(p.contents) - 2000 * 4, C.POINTER(C.c_float))
+    buf = np.ctypeslib.as_array(base, shape=(n + 4000,)).copy()
+    L.freeData(p)
+    assert np.array_equal(buf[2000:2000 + n], x)
+    assert not buf[:2000].any() and not buf[2000 + n:].any()
+    empty = tmp_path / "empty.dat"
+    empty.write_bytes(b"")
+    assert L.readData(str(empty).encode(), C.byref(p)) == 0 and L.accel_compat_status() < 0
+    big = tmp_path / "big.dat"
+    with open(big, "wb") as fh:
+        fh.truncate(((1 << 26) + 1) * 4)  # sparse: one sample over the limit
+    assert L.readData(str(big).encode(), C.byref(p)) == 0 and L.accel_compat_status() < 0
+    assert L.readData(str(tmp_path / "missing.dat").encode(), C.byref(p)) == 0
+    assert L.accel_compat_status() < 0
