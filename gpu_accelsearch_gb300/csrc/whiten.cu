@@ -79,8 +79,150 @@ __global__ void __launch_bounds__(256) k_whiten_scale(const int* __restrict__ bs
     }
 }
 
+// Warp-per-block forms of the two kernels for blocks of at most
+// kWarpBlockMax bins (the reference's widths are at most 200): eight
+// whitening blocks per CTA, no CTA-wide barriers.
+constexpr int kWarpBlockMax = 1024;
+constexpr int kWarpsPerCta = 8;
+
+// Exact rank-k key of keys[0..n) by an 8-bit radix select within one warp
+// (hist: 256 ints of this warp's shared memory).
+__device__ __forceinline__ uint32_t warp_select_u32(const uint32_t* keys, int n, int k, int* hist) {
+    const int lane = threadIdx.x & 31;
+    uint32_t prefix = 0, mask = 0;
+#pragma unroll 1
+    for (int shift = 24; shift >= 0; shift -= 8) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) hist[lane * 8 + j] = 0;
+        __syncwarp();
+        for (int i0 = 0; i0 < n; i0 += 32) {
+            const int i = i0 + lane;
+            bool act = false;
+            uint32_t d = 0;
+            if (i < n) {
+                const uint32_t key = keys[i];
+                act = (key & mask) == prefix;
+                d = (key >> shift) & 255u;
+            }
+            // aggregate equal digits before the shared-memory atomic
+            const unsigned am = __ballot_sync(0xffffffffu, act);
+            if (act) {
+                const unsigned peers = __match_any_sync(am, d);
+                if (lane == __ffs(peers) - 1) atomicAdd(&hist[d], __popc(peers));
+            }
+        }
+        __syncwarp();
+        int loc[8], sum = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            loc[j] = hist[lane * 8 + j];
+            sum += loc[j];
+        }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int excl = incl - sum;
+        int digit = 0, knew = 0;
+        const bool mine = k >= excl && k < incl;
+        if (mine) {
+            int c = excl;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (k >= c && k < c + loc[j]) {
+                    digit = lane * 8 + j;
+                    knew = k - c;
+                }
+                c += loc[j];
+            }
+        }
+        const int src = __ffs(__ballot_sync(0xffffffffu, mine)) - 1;
+        digit = __shfl_sync(0xffffffffu, digit, src);
+        k = __shfl_sync(0xffffffffu, knew, src);
+        prefix |= (uint32_t)digit << shift;
+        mask |= 255u << shift;
+        __syncwarp();
+    }
+    return prefix;
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_medians_warp(const int* __restrict__ bstart,
+                                                                           const int* __restrict__ blen,
+                                                                           const float2* __restrict__ spec,
+                                                                           double* med, int nblocks, int maxlen) {
+    extern __shared__ uint32_t wsm[];  // per warp: 256 histogram ints, then maxlen keys
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarpsPerCta + w;
+    if (b >= nblocks) return;  // whole warps leave; nothing below synchronises the CTA
+    int* hist = reinterpret_cast<int*>(wsm + (size_t)w * (256 + maxlen));
+    uint32_t* keys = wsm + (size_t)w * (256 + maxlen) + 256;
+    const int s = bstart[b], n = blen[b];
+    for (int i = lane; i < n; i += 32) keys[i] = __float_as_uint(power_exact(spec[s + i]));
+    __syncwarp();
+    const uint32_t k = warp_select_u32(keys, n, (n - 1) / 2, hist);
+    if (lane == 0) med[b] = (double)__uint_as_float(k) / kLn2w;
+}
+
+// Write range r as in k_whiten_scale, one warp per range.
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_scale_warp(const int* __restrict__ bstart,
+                                                                         const int* __restrict__ blen,
+                                                                         const double* __restrict__ med, int nb,
+                                                                         float2* spec, unsigned numbins) {
+    const int r = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (r > nb) return;
+    long long lo, hi;
+    float mean_old, dslope;
+    if (r == 0) {
+        lo = 1;
+        hi = bstart[0] + blen[0] / 2;
+        mean_old = (float)med[0];
+        dslope = 0.f;
+        if (lane == 0) spec[0] = make_float2(1.0f, 0.0f);
+    } else if (r < nb) {
+        lo = bstart[r - 1] + blen[r - 1] / 2;
+        hi = bstart[r] + blen[r] / 2;
+        mean_old = (float)med[r - 1];
+        dslope = (float)((med[r] - (double)mean_old) / (0.5 * (blen[r - 1] + blen[r])));
+    } else {
+        lo = bstart[nb - 1] + blen[nb - 1] / 2;
+        hi = numbins;
+        mean_old = (float)med[nb - 1];
+        if (nb >= 2) {
+            const float mo = (float)med[nb - 2];
+            dslope = (float)((med[nb - 1] - (double)mo) / (0.5 * (blen[nb - 2] + blen[nb - 1])));
+        } else {
+            dslope = 1.0f;
+        }
+    }
+    const float flat = rsqrt_magic(mean_old);
+    for (long long ind = lo + lane; ind < hi; ind += 32) {
+        float norm;
+        if (r == 0) norm = flat;
+        else norm = rsqrt_magic(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))));
+        float2 v = spec[ind];
+        v.x = __fmul_rn(v.x, norm);
+        v.y = __fmul_rn(v.y, norm);
+        spec[ind] = v;
+    }
+}
+
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
                   unsigned numbins, int maxlen, cudaStream_t st) {
+    if (maxlen <= kWarpBlockMax) {
+        const size_t smem = sizeof(uint32_t) * (size_t)kWarpsPerCta * (256 + maxlen);
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k_whiten_medians_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        k_whiten_medians_warp<<<(nblocks + kWarpsPerCta - 1) / kWarpsPerCta, 32 * kWarpsPerCta, smem, st>>>(
+            d_bstart, d_blen, spec, d_med, nblocks, maxlen);
+        if (cudaGetLastError() != cudaSuccess) return -1;
+        k_whiten_scale_warp<<<(nblocks + kWarpsPerCta) / kWarpsPerCta, 32 * kWarpsPerCta, 0, st>>>(
+            d_bstart, d_blen, d_med, nblocks, spec, numbins);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
     size_t smem = sizeof(uint32_t) * (size_t)maxlen;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(k_whiten_medians, cudaFuncAttributeMaxDynamicSharedMemorySize,

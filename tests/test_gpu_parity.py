@@ -70,7 +70,8 @@ def test_bank_spectra(S):
 
 
 @pytest.mark.parametrize("numbins,init,maxb", [(1 << 17, 6, 200), (1 << 15, 6, 200),
-                                               (12345, 6, 200), (1 << 17, 1000, 1000)])
+                                               (12345, 6, 200), (1 << 17, 1000, 1000),
+                                               (1 << 17, 2000, 2000), (1 << 16, 3, 2000)])
 def test_whitening_bit_exact(numbins, init, maxb):
     from gpu_accelsearch_gb300.search import AccelSearch
     spec = synth_red_spectrum(numbins + 1, seed=numbins)
