@@ -100,6 +100,7 @@ struct HsumArgs {
     float* stage_out;       // optional [nseg][nstages][numzs0][uselen]
     int nstages;
     unsigned long long* err;  // bit 0: a tile's copy wait timed out
+    int tile_floats;          // largest shared-memory footprint of a tile (host-proven)
 };
 
 // Fundamental plane fused with the harmonic sum (k_fund_sum).

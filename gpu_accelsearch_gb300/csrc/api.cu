@@ -538,6 +538,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ha.stage_out = stage_out;
         ha.nstages = c->nstages;
         ha.err = c->d_ncand + 1;
+        ha.tile_floats = c->tile_floats;
         ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;

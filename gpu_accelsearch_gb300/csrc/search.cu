@@ -37,7 +37,7 @@ static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t 
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess ||
+                                 (int)(sizeof(float) * kTileSmemFloats)) != cudaSuccess ||
             cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
@@ -85,7 +85,11 @@ int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st) {
 
 int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st) {
     dim3 grid((a.uselen + kTileI - 1) / kTileI, (a.numzs0 + kTileZ - 1) / kTileZ, nseg);
-    const size_t smem = sizeof(float) * kTileSmemFloats;
+    // the plan's own worst tile (at most kTileSmemFloats): a smaller
+    // footprint fits more CTAs per SM (4 instead of 3 at zmax 200, 8 harmonics)
+    const int floats = (a.tile_floats > 0 && a.tile_floats <= kTileSmemFloats) ? ((a.tile_floats + 3) & ~3)
+                                                                                : kTileSmemFloats;
+    const size_t smem = sizeof(float) * floats;
     const bool so = a.stage_out != nullptr;
     switch (a.nh) {
         case 1: return so ? hsum_tile_nh<1, true>(a, grid, smem, st) : hsum_tile_nh<1, false>(a, grid, smem, st);

@@ -354,7 +354,7 @@ __host__ __device__ constexpr int stage_after(int h) {
 }
 
 template <int NH, bool STAGE_OUT>
-__global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
+__global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
     static_assert(NH <= 32, "one lane per harmonic");
     extern __shared__ __align__(128) float tsm[];
     __shared__ __align__(16) int s_row[NH][kTileZ];  // byte offset of the row used by tile row zr
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kTileI, 3) k_hsum_tile(const HsumArgs a) {
 #pragma unroll
     for (int h = 0; h < NH; h++) {
         if (h == 0) {
-            colb[h] = 4 * tid;
+            colb[h] = valid ? 4 * tid : 0;  // lanes past the plane edge read column 0
         } else {
             const HarmPlan& H = a.h[h];
             const int c0 = s_c0[h];
@@ -668,7 +668,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a,
 #pragma unroll
         for (int h = 0; h < NH; h++) {
             if (h == 0) {
-                colb[h] = 4 * c;
+                colb[h] = valid ? 4 * c : 0;
             } else {
                 const HarmPlan& H = a.h[h];
                 const int c0 = s_c0[b][h];
