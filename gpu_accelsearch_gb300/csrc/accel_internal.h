@@ -140,6 +140,8 @@ int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st);
 constexpr int kHsumTileZ = 16;
 constexpr int kHsumTileI = 256;
 constexpr int kHsumTileFloats = 15360;
+constexpr int kPipeBuffers = 4;   // tile buffers of the pipelined harmonic sum
+constexpr int kPipeSmemMax = 222 * 1024;  // their dynamic shared memory (227 KB less the static tables)
 
 // Record an error message for accel_last_error() and return `code`.
 int set_error(int code, const char* fmt, ...);

@@ -542,7 +542,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
-        if (c->tile_ok && c->hsum_tiled && c->hsum_pipe)
+        if (c->tile_ok && c->hsum_tiled && c->hsum_pipe && 4LL * ((c->tile_floats + 31) & ~31) * kPipeBuffers <= kPipeSmemMax)
             CKL(launch_hsum_pipe(ha, nseg, sum_stream), "harmonic sum (tiled, pipelined)");
         else if (c->tile_ok && c->hsum_tiled)
             CKL(launch_hsum_tile(ha, nseg, sum_stream), "harmonic sum (tiled)");

@@ -50,10 +50,14 @@ static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t 
 template <int NH, bool SO>
 static int hsum_pipe_nh(const HsumArgs& a, int ntiles, cudaStream_t st) {
     static bool attr = false;
-    const size_t smem = sizeof(float) * kTileSmemFloats * kPipeBufs;
+    // buffers of the plan's worst tile, 128-byte aligned
+    const int bstride = (a.tile_floats > 0 && a.tile_floats <= kTileSmemFloats) ? ((a.tile_floats + 31) & ~31)
+                                                                                 : kTileSmemFloats;
+    const size_t smem = sizeof(float) * (size_t)bstride * kPipeBufs;
+    if (smem > (size_t)kPipeSmemMax) return -1;  // the caller checks this before choosing the kernel
     if (!attr) {
         if (cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess ||
+                                 kPipeSmemMax) != cudaSuccess ||
             cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
@@ -64,7 +68,7 @@ static int hsum_pipe_nh(const HsumArgs& a, int ntiles, cudaStream_t st) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return -1;
     const int grid = std::max(1, std::min(ntiles, sms));
-    k_hsum_pipe<NH, SO><<<grid, kPipeThreads, smem, st>>>(a, ntiles);
+    k_hsum_pipe<NH, SO><<<grid, kPipeThreads, smem, st>>>(a, ntiles, bstride);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
 
 // ------------------------------------------------------- pipelined tiled hsum
 // The same tiles and sums as k_hsum_tile, from one persistent CTA per SM
-// with kPipeBufs tile buffers in shared memory and specialised warps: one
+// with kPipeBufs tile buffers (each the plan's worst tile) in shared memory and specialised warps: one
 // producer warp computes each tile's rectangles and issues its bulk copies
 // (completing on the buffer's "full" mbarrier) as soon as the consumers
 // have released the buffer (its "empty" mbarrier); 16 consumer warps, two
@@ -538,15 +538,15 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
 // of the next tiles overlap the additions of the current one.  Every wait
 // is bounded; a warp that gives up sets the error word, lets the copies it
 // knows of land, and leaves.
-constexpr int kPipeBufs = 3;
+constexpr int kPipeBufs = kPipeBuffers;
 constexpr int kPipeConsumers = 2 * kTileI;                 // 512 threads, 16 warps
 constexpr int kPipeThreads = kPipeConsumers + 32 * kPipeBufs;  // + one producer warp per buffer
 
 template <int NH, bool STAGE_OUT>
-__global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a, int ntiles) {
+__global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a, int ntiles, int bstride) {
     static_assert(NH <= 32, "one lane per harmonic");
     static_assert(kTileZ == 16 && kTileI == 256, "two threads per column, 8 rows each");
-    extern __shared__ __align__(128) float tsm[];  // kPipeBufs x kTileSmemFloats
+    extern __shared__ __align__(128) float tsm[];  // kPipeBufs buffers of bstride floats
     __shared__ __align__(16) int s_row[kPipeBufs][NH][kTileZ];  // byte offset of tile row zr's row
     __shared__ int s_c0[kPipeBufs][NH], s_cb[kPipeBufs][NH], s_crem[kPipeBufs][NH];
     __shared__ int s_tile[kPipeBufs][4];  // seg, z0, i0, nz | ni << 16
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a,
             if (lane < NH) {
                 const HarmPlan& H = a.h[lane];
                 const float* src = a.planes + (long long)seg * a.pstride + H.poff + (long long)zf * H.prow + c0;
-                float* dst = tsm + b * kTileSmemFloats + off;
+                float* dst = tsm + b * bstride + off;
                 for (int r = 0; r < nzr; r++)
                     bulk_copy_g2s(dst + 4 * w4 * r, src + (long long)r * H.prow, 16u * (unsigned)w4, &s_full[b]);
             }
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_hsum_pipe(const HsumArgs a,
                 colb[h] = valid ? 4 * (rind - c0) : 0;
             }
         }
-        const char* tb = reinterpret_cast<const char*>(tsm + b * kTileSmemFloats);
+        const char* tb = reinterpret_cast<const char*>(tsm + b * bstride);
         int ro[NH][kTileZ / 2];
 #pragma unroll
         for (int h = 0; h < NH; h++)
