@@ -190,13 +190,26 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
     constexpr int Q = 16 / R;
     constexpr int PM = FftShape<M>::PADDED;
     if constexpr (!FIRST) {
-#pragma unroll
-        for (int nb = 0; nb < NB; nb++)
+        if constexpr (NB == 2) {
+            // both transforms' values of one index side by side: one 16-byte access
+            const float4* sm4 = reinterpret_cast<const float4*>(sm);
 #pragma unroll
             for (int q = 0; q < Q; q++)
 #pragma unroll
-                for (int r = 0; r < R; r++)
-                    a[nb][q + r * Q] = sm[nb * PM + fft_pad(t + q * T + r * (M / R))];
+                for (int r = 0; r < R; r++) {
+                    const float4 v = sm4[fft_pad(t + q * T + r * (M / R))];
+                    a[0][q + r * Q] = make_float2(v.x, v.y);
+                    a[1][q + r * Q] = make_float2(v.z, v.w);
+                }
+        } else {
+#pragma unroll
+            for (int nb = 0; nb < NB; nb++)
+#pragma unroll
+                for (int q = 0; q < Q; q++)
+#pragma unroll
+                    for (int r = 0; r < R; r++)
+                        a[nb][q + r * Q] = sm[nb * PM + fft_pad(t + q * T + r * (M / R))];
+        }
         __syncthreads();
     }
 #pragma unroll
@@ -218,15 +231,24 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
             }
         }
 #pragma unroll
-        for (int nb = 0; nb < NB; nb++) {
-            dft<R, DIR>(v[nb]);
-            if constexpr (LAST) {
+        for (int nb = 0; nb < NB; nb++) dft<R, DIR>(v[nb]);
+        if constexpr (LAST) {
+#pragma unroll
+            for (int nb = 0; nb < NB; nb++)
 #pragma unroll
                 for (int r = 0; r < R; r++) a[nb][q + r * Q] = v[nb][r];
-            } else {
-                const int j = (b / NS) * (NS * R) + k;
+        } else {
+            const int j = (b / NS) * (NS * R) + k;
+            if constexpr (NB == 2) {
+                float4* sm4 = reinterpret_cast<float4*>(sm);
 #pragma unroll
-                for (int r = 0; r < R; r++) sm[nb * PM + fft_pad(j + r * NS)] = v[nb][r];
+                for (int r = 0; r < R; r++)
+                    sm4[fft_pad(j + r * NS)] = make_float4(v[0][r].x, v[0][r].y, v[1][r].x, v[1][r].y);
+            } else {
+#pragma unroll
+                for (int nb = 0; nb < NB; nb++)
+#pragma unroll
+                    for (int r = 0; r < R; r++) sm[nb * PM + fft_pad(j + r * NS)] = v[nb][r];
             }
         }
     }
@@ -235,9 +257,11 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
 
 // Full transform: radix-16 passes, the leftover factor (2, 4 or 8) last.
 // t is the thread's index within the group of M/16 threads doing the
-// transform(s); sm must hold NB * FftShape<M>::PADDED float2.  The
-// twiddles of the radix-16 passes after the first are loaded up front.
-// Shared memory may be rewritten as soon as this returns.
+// transform(s); sm (16-byte aligned) must hold NB * FftShape<M>::PADDED
+// float2 -- for two transforms as PADDED float4, both transforms' values
+// of an index side by side.  The twiddles of the radix-16 passes after the
+// first are loaded up front.  Shared memory may be rewritten as soon as
+// this returns.
 template <int M, int DIR, int NB>
 __device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const float2* __restrict__ tw,
                                         int t) {
