@@ -3,6 +3,8 @@
 // (include/accelsearch.h).
 #pragma once
 
+#include <atomic>
+
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -125,6 +127,16 @@ struct FundArgs {
     float* stage_out;       // optional [nseg][nstages][numzs0][uselen]
     int nstages;
 };
+
+// Kernel attributes (dynamic shared memory, carveout) are per device: a
+// launcher keeps one bit per device it has configured.
+inline bool attr_pending(const std::atomic<unsigned long long>& done, int* dev) {
+    if (cudaGetDevice(dev) != cudaSuccess) *dev = 64;
+    return *dev >= 64 || !((done.load() >> *dev) & 1ull);
+}
+inline void attr_set(std::atomic<unsigned long long>& done, int dev) {
+    if (dev < 64) done.fetch_or(1ull << dev);
+}
 
 // ---- launchers (return 0 or -1 after a launch error) ----
 int launch_fund_sum(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st);

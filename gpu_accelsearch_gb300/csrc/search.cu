@@ -34,14 +34,15 @@ int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st) {
 
 template <int NH, bool SO>
 static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr{0};
+    int dev = 0;
+    if (attr_pending(attr, &dev)) {
         if (cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(float) * kTileSmemFloats)) != cudaSuccess ||
             cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
-        attr = true;
+        attr_set(attr, dev);
     }
     k_hsum_tile<NH, SO><<<grid, kTileI, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -49,21 +50,22 @@ static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t 
 
 template <int NH, bool SO>
 static int hsum_pipe_nh(const HsumArgs& a, int ntiles, cudaStream_t st) {
-    static bool attr = false;
+    static std::atomic<unsigned long long> attr{0};
+    int dev = 0;
     // buffers of the plan's worst tile, 128-byte aligned
     const int bstride = (a.tile_floats > 0 && a.tile_floats <= kTileSmemFloats) ? ((a.tile_floats + 31) & ~31)
                                                                                  : kTileSmemFloats;
     const size_t smem = sizeof(float) * (size_t)bstride * kPipeBufs;
     if (smem > (size_t)kPipeSmemMax) return -1;  // the caller checks this before choosing the kernel
-    if (!attr) {
+    if (attr_pending(attr, &dev)) {
         if (cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kPipeSmemMax) != cudaSuccess ||
             cudaFuncSetAttribute(k_hsum_pipe<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
-        attr = true;
+        attr_set(attr, dev);
     }
-    int dev = 0, sms = 0;
+    int sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return -1;

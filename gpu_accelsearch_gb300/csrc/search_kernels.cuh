@@ -810,14 +810,15 @@ __global__ void __launch_bounds__(kHsumCols) k_hsum(const HsumArgs a) {
 // -------------------------------------------------------------- launchers
 template <int M> static int prep_m(const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st) {
     size_t smem = sizeof(float2) * FftShape<M>::PADDED + sizeof(uint32_t) * M;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr{0};
+    int dev = 0;
+    if (attr_pending(attr, &dev)) {
         if (cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
-        attr = true;
+        attr_set(attr, dev);
     }
     k_prep<M><<<dim3(a.nh, nseg), M / 16, smem, st>>>(a, tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -826,14 +827,15 @@ template <int M> static int prep_m(const PrepArgs& a, int nseg, const float2* tw
 template <int M, bool F16, bool SPLIT>
 static int plane_m(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st) {
     size_t smem = sizeof(float2) * FftShape<M>::PADDED * PlaneShape<SPLIT, M>::BUFFERS;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr{0};
+    int dev = 0;
+    if (attr_pending(attr, &dev)) {
         if (cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess ||
             cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
-        attr = true;
+        attr_set(attr, dev);
     }
     k_plane<M, F16, SPLIT><<<dim3(nseg, a.ntpl), PlaneShape<SPLIT, M>::THREADS, smem, st>>>(a, tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
@@ -849,14 +851,15 @@ static int plane_dispatch(const PlaneArgs& a, int nseg, const float2* tw, cudaSt
 template <int M, bool F16>
 static int fund_m(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st) {
     size_t smem = sizeof(float2) * FftShape<M>::PADDED * 2;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr{0};
+    int dev = 0;
+    if (attr_pending(attr, &dev)) {
         if (cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess ||
             cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
-        attr = true;
+        attr_set(attr, dev);
     }
     k_fund_sum<M, F16><<<dim3(a.h[0].numzs, nseg), PlaneShape<false, M>::THREADS, smem, st>>>(a, tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
