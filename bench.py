@@ -520,6 +520,23 @@ def run_ours(args):
                     "per_kernel": {n: {"achieved_GBs": round(v["achieved"], 1),
                                        "frac": round(v["achieved"] / peak, 4)}
                                    for n, v in per_kernel.items()}}
+    # the compute side of the plane kernel: algorithmic FP32 work of every
+    # row (two M-point inverse FFTs at 5 M log2 M flops each, the complex
+    # template products and the powers) over the same CUDA-event time,
+    # against the nominal FP32 rate (SMs x 128 lanes x 2 flops x max clock;
+    # no measured FP32 peak exists for this machine)
+    if roofline is not None and "plane" in per_kernel and not fused:
+        import math
+        flops_seg = sum(h.numzs * (2 * 5 * (h.fftlen // 2) * math.log2(h.fftlen // 2) + 18 * (h.fftlen // 2))
+                        for h in s.harmonics)
+        props = torch.cuda.get_device_properties(local)
+        mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+        fp32_peak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+        achieved_tf = flops_seg * segs / (k["plane"]["ms"] / 1e3) / 1e12
+        roofline["fp32_side"] = {"kernel": "k_plane", "flops_per_segment": flops_seg,
+                                 "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": achieved_tf / fp32_peak,
+                                 "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock"}
     step_roofline = {"bytes_per_cell": bytes_per_cell,
                      "achieved": value / world * bytes_per_cell / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": value / world * bytes_per_cell / 1e9 / peak,
