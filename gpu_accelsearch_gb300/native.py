@@ -103,6 +103,9 @@ SIGNATURES = {
                                C.c_int, _llp]),
     "accel_search_spectra": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), _llp, _llp, _llp]),
     "accel_candidates": (C.c_int, [_vp, C.POINTER(Candidate), _ll, _llp]),
+    "accel_sift_candidates": (C.c_int, [C.POINTER(Candidate), C.c_longlong, C.c_double, C.c_int,
+                                        C.c_double, C.POINTER(Candidate), C.c_longlong,
+                                        C.POINTER(C.c_longlong)]),
     "accel_whiten": (C.c_int, [_vp, _vp, _ll]),
     "accel_rfft": (C.c_int, [_vp, _vp, _ll, _vp]),
     "accel_prepare_segments": (C.c_int, [_vp, _vp, _ll, _llp, C.c_int, _vp]),

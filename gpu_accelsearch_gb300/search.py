@@ -48,6 +48,35 @@ CAND_DTYPE = np.dtype([("trial", "i4"), ("step", "i4"), ("r", "f8"), ("z", "f8")
                        ("numharm", "i4"), ("power", "f4"), ("sigma", "f4")])
 
 
+def _to_native(cands: np.ndarray):
+    buf = (N.Candidate * max(len(cands), 1))()
+    for k, c in enumerate(cands):
+        buf[k].trial, buf[k].step = int(c["trial"]), int(c["step"])
+        buf[k].r, buf[k].z = float(c["r"]), float(c["z"])
+        buf[k].numharm, buf[k].power, buf[k].sigma = int(c["numharm"]), float(c["power"]), float(c["sigma"])
+    return buf
+
+
+def _from_native(buf, n: int) -> np.ndarray:
+    out = np.zeros(n, CAND_DTYPE)
+    for k in range(n):
+        c = buf[k]
+        out[k] = (c.trial, c.step, c.r, c.z, c.numharm, c.power, c.sigma)
+    return out
+
+
+def sift_candidates(cands: np.ndarray, min_dr: float = 15.0, maxharm: int = 8,
+                    harm_dr: float = 1.0) -> np.ndarray:
+    """accel_sift_candidates on a CAND_DTYPE array (see accelsearch.h)."""
+    n = len(cands)
+    src = _to_native(cands)
+    dst = (N.Candidate * max(n, 1))()
+    m = C.c_longlong()
+    N.check(N.lib().accel_sift_candidates(src, n, float(min_dr), int(maxharm), float(harm_dr), dst,
+                                          n, C.byref(m)))
+    return _from_native(dst, m.value)
+
+
 def first_bin(nsamples: int, dt: float) -> int:
     return N.lib().accel_first_bin(nsamples, dt)
 

@@ -178,6 +178,16 @@ int  accel_search_spectra(accel_ctx *ctx, int ntrials, const accel_complex *cons
                           const long long *numbins, const long long *rlo, long long *ncand);
 /* Candidates of the last search, sorted by (trial, step, numharm, z, r). */
 int  accel_candidates(accel_ctx *ctx, accel_candidate *out, long long cap, long long *n);
+/* Candidate sifting, host only (the reference's sortCandidates and
+ * eliminateHarmonics stubs, bpd_candidates.cu:15-33, AccelSearch.cu:290-305).
+ * Per trial: order by sigma (descending; ties by power, then r, z,
+ * numharm); keep a candidate only if no kept one is strictly closer than
+ * min_dr bins in r (any z or harmonic count); then, when maxharm > 1, drop
+ * a kept candidate whose r is within harm_dr bins of (a/b) times a stronger
+ * kept candidate's r, 1 <= a, b <= maxharm, a != b.  Output ordered by
+ * trial, then sigma; *nout = survivors (at most cap written). */
+int  accel_sift_candidates(const accel_candidate *in, long long n, double min_dr, int maxharm,
+                           double harm_dr, accel_candidate *out, long long cap, long long *nout);
 
 /* ------------------------------------------------------------ stage calls */
 /* Whitening in place (deredden, bpd_noise.c:12-92). */

@@ -242,3 +242,37 @@ def fft64(x, sign=-1):
     a = np.array(x, dtype=np.complex128, copy=True)
     lib().orc_fft(_dp(a.view(np.float64)), a.size, sign)
     return a
+
+
+def sift(cands, min_dr=15.0, maxharm=8, harm_dr=1.0):
+    """Candidate sifting restated with plain loops (small cases only): per
+    trial, by sigma (then power, r, z, numharm); drop a candidate strictly
+    closer than min_dr in r to a kept one; then drop one within harm_dr of
+    (a/b) times a stronger survivor's r, 1 <= a, b <= maxharm, a != b, a/b
+    in lowest terms.  Returns the survivors in that order."""
+    from math import gcd
+    ratios = [(a, b) for a in range(1, maxharm + 1) for b in range(1, maxharm + 1)
+              if a != b and gcd(a, b) == 1]
+    order = sorted(range(len(cands)), key=lambda k: (
+        int(cands[k]["trial"]), -float(cands[k]["sigma"]), -float(cands[k]["power"]),
+        float(cands[k]["r"]), float(cands[k]["z"]), int(cands[k]["numharm"])))
+    out = []
+    trials = sorted({int(c["trial"]) for c in cands})
+    for t in trials:
+        group = []
+        for k in order:
+            c = cands[k]
+            if int(c["trial"]) != t:
+                continue
+            if min_dr > 0 and any(abs(float(g["r"]) - float(c["r"])) < min_dr for g in group):
+                continue
+            group.append(c)
+        final = []
+        for c in group:
+            harmonic = maxharm > 1 and any(
+                abs(float(c["r"]) - a / b * float(f["r"])) <= harm_dr
+                for f in final for a, b in ratios)
+            if not harmonic:
+                final.append(c)
+        out.extend(final)
+    return out

@@ -86,3 +86,21 @@ def test_batch_of_uneven_trials_equals_alone(big):
     mine["trial"] = 0
     key = ["step", "numharm", "z", "r"]
     assert np.array_equal(np.sort(alone, order=key), np.sort(mine, order=key))
+
+
+def test_sift_keeps_each_signal_once(big):
+    # sifting (min_dr 15 bins, harmonics up to 8) leaves far fewer candidates,
+    # and every injected signal -- or a harmonic alias of it, which the sum
+    # stages also flag -- survives
+    from math import gcd
+    from gpu_accelsearch_gb300.search import sift_candidates
+    s, x = big["s"], big["x"]
+    s.search([x], DT)
+    c = s.candidates()
+    kept = sift_candidates(c, min_dr=15.0, maxharm=8, harm_dr=1.0)
+    assert 0 < len(kept) < len(c) / 5
+    ratios = [(a, b) for a in range(1, 9) for b in range(1, 9) if gcd(a, b) == 1]
+    for amp, r0, z in big["sigs"]:
+        rs = r0 + z / 2
+        hit = [k for k in kept if any(abs(k["r"] - a / b * rs) <= 2.0 for a, b in ratios)]
+        assert hit, (r0, z)
