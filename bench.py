@@ -315,7 +315,7 @@ def cpu_baseline(seconds: float):
     el = time.perf_counter() - t
     cells = nsteps * U * int(orc.geom[0, 3])
     orc.close()
-    return {"value": cells / el, "unit": "cells/s", "cores": cores, "kind": "port",
+    return {"value": cells / el, "unit": "cells/s", "cores": cores, "kind": "port", "seconds": el,
             "sample": f"{nsteps} overlap-save steps of one 2^22-sample trial (zmax=200, 8 "
                       f"harmonics, L=8192, uselen=7734): FP64 oracle planes + harmonic sum + "
                       f"threshold, {el:.1f} s"}
@@ -328,12 +328,14 @@ def run_reference(args):
     per = max(1.0, args.cpu_seconds / 3)
     for _ in range(args.warmup):
         cpu_baseline(per / 4)
-    vals = [cpu_baseline(per)["value"] for _ in range(args.steps)]
-    cb = cpu_baseline(per)
-    v = float(np.median(vals))
+    runs = [cpu_baseline(per) for _ in range(max(1, args.steps))]
+    v = float(np.median([r["value"] for r in runs]))
+    cb = dict(runs[-1])
     cb["value"] = v
+    # one step = one bounded sample of the workload (the sample is in cpu_baseline)
+    ms = 1e3 * float(np.median([r["seconds"] for r in runs]))
     line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded N(0,1) float32 series with an injected sinusoid",
             "impl": "reference",
