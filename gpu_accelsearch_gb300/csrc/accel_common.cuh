@@ -22,6 +22,7 @@ constexpr int kMaxHarm = 16;        // harmonics per bank (numharm <= 16)
 constexpr int kMaxStages = 5;       // 1,2,4,8,16
 constexpr int kNumBetween = 2;      // interbinning (bpd_common.h:30)
 constexpr int kDz = 2;              // f-dot step (bpd_common.h:33)
+constexpr double kLn2 = 0.693147180559945309417232121458;  // median -> mean of an exponential
 constexpr int kFintBins = 16;       // NUMFINTBINS (bpd_common.h:45)
 constexpr int kTwN = 8192;          // twiddle table length (max FFT points)
 constexpr int kMinM = 64;           // smallest half-length FFT

@@ -138,9 +138,32 @@ inline void attr_set(std::atomic<unsigned long long>& done, int dev) {
     if (dev < 64) done.fetch_or(1ull << dev);
 }
 
+// Candidate refinement (k_optimize in bank.cu): one CTA per candidate.
+struct OptCand {
+    double r, z;            // fundamental-plane frequency and f-dot of the candidate
+    int numharm;            // harmonics k r / numharm, k = 1..numharm, are summed
+    int trial;
+    long long lobin[kMaxHarm];  // harmonic k's segment in the candidate's step:
+    int numdata[kMaxHarm];      // its median sets the power normalisation
+};
+struct OptOut {
+    double r, z, power;     // refined position and summed power
+    float harm[kMaxHarm];   // power of harmonic k at the refined position
+};
+struct OptArgs {
+    const float2* const* spec;   // [ntrials] whitened spectra (device)
+    const long long* numbins;    // [ntrials]
+    const OptCand* in;
+    OptOut* out;
+    int n;
+    int refine;                  // 0: evaluate at the given position only
+    int maxdata;                 // largest numdata (shared-memory keys)
+};
+
 // ---- launchers (return 0 or -1 after a launch error) ----
 int launch_fund_sum(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_twiddles(float2* tw, cudaStream_t st);
+int launch_optimize(const OptArgs& a, cudaStream_t st);
 int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int nh, int ntpl,
                       float2* resp, int rstride, bool fp16, cudaStream_t st);
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);

@@ -1010,8 +1010,10 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
         if (rc) return rc;
         specs[i] = t.spec;
         nb[i] = n / 2;
+        t.numbins = n / 2;
         rlo[i] = accel_first_bin(n, dt[i]);
     }
+    c->last_trials = ntrials;
     rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data());
     if (ncand) *ncand = (long long)c->last_raw;
     return rc;

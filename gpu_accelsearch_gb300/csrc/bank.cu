@@ -282,4 +282,164 @@ int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int
     return 0;
 }
 
+
+// --------------------------------------------------------------------------
+// Candidate refinement (the reference's optimizeCandidates stub,
+// bpd_candidates.cu:24-27).
+//
+// The power the plane kernels compute at fundamental-plane position
+// (r, z) is |sum_j X[j] conj(F(r - j - z/2; z))|^2 over the 2 hw(z) bins
+// j in [ceil(r - hw), ceil(r + hw)), where F is the response that
+// generate_z_response samples (bpd_subharmonics.cu:146-226; its loop
+// variable is the argument x) and X the whitened spectrum: the planes are
+// this expression on the grid r = rlo + i/2, z even.  Here it is evaluated
+// at any (r, z), for every harmonic k r / H, k z / H (k = 1..H) of a
+// candidate, and the summed power is maximised on three nested 5 x 5 grids
+// (steps 1/4, 1/16, 1/64 in r and 1, 1/4, 1/16 in z around the best point
+// so far).
+// F(x; z), evaluated directly (the reference's small-offset series
+// corrections are expansions of the same function).
+__device__ double2 response_at(double x, double z) {
+    if (fabs(z) < 1e-4) {  // generate_r_response: e^{i pi x} sin(pi x) / (pi x)
+        const double px = kPi * x;
+        double s, c;
+        sincos(px, &s, &c);
+        const double sinc = (x == 0.0) ? 1.0 : s / px;
+        return make_double2(c * sinc, s * sinc);
+    }
+    const double absz = fabs(z);
+    const int signz = (z < 0) ? -1 : 1;
+    const double zd = signz * kSqrt2 / sqrt(absz);
+    const double cons = zd / 2.0;
+    const double yy = x * zd;
+    const double zz = yy + z * zd;
+    const double xx = kPi / z * x * x;
+    const double c = cos(xx), s = sin(xx);
+    double fsy, fcy, fsz, fcz;
+    fresnel(yy, &fsy, &fcy);
+    fresnel(zz, &fsz, &fcz);
+    const double tre = signz * (fcz - fcy);
+    const double tim = fsy - fsz;
+    return make_double2((tre * c - tim * s) * cons, -(tre * s + tim * c) * cons);
+}
+
+// Power of one harmonic at (r, z), summed by one warp.
+__device__ double warp_power(const float2* __restrict__ X, long long nb, double r, double z, int lane) {
+    const int hw = z_halfwidth(z);
+    const long long j0 = (long long)ceil(r - hw);
+    const double base = r - 0.5 * z;
+    double re = 0.0, im = 0.0;
+    for (int i = lane; i < 2 * hw; i += 32) {
+        const long long j = j0 + i;
+        if (j < 0 || j >= nb) continue;
+        const double2 w = response_at(base - (double)j, z);
+        const float2 v = X[j];
+        // X[j] * conj(w)
+        re += (double)v.x * w.x + (double)v.y * w.y;
+        im += (double)v.y * w.x - (double)v.x * w.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    return re * re + im * im;
+}
+
+constexpr int kOptWarps = 4;
+
+__global__ void __launch_bounds__(32 * kOptWarps) k_optimize(const OptArgs a) {
+    extern __shared__ uint32_t okeys[];  // a.maxdata keys
+    const int ci = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const OptCand& cand = a.in[ci];
+    const float2* __restrict__ X = a.spec[cand.trial];
+    const long long nb = a.numbins[cand.trial];
+    const int H = cand.numharm;
+    __shared__ double s_pow[25];
+    __shared__ double s_best[3];  // r, z, power
+    __shared__ double s_n2[kMaxHarm];
+    __shared__ int hist[256];
+    __shared__ int bc[2];
+    // every harmonic's power normalisation, as the search applies it to the
+    // candidate's step: the squared magic rsqrt of the segment's median
+    // power / ln 2 (bpd_search.cu:144-181)
+    for (int k = 0; k < H; k++) {
+        const int nd = cand.numdata[k];
+        const long long lo = cand.lobin[k];
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            const long long b = lo + i;
+            const float2 v = (b >= 0 && b < nb) ? X[b] : make_float2(0.f, 0.f);
+            okeys[i] = __float_as_uint(power_exact(v));
+        }
+        __syncthreads();
+        const uint32_t mk = block_select_u32(okeys, nd, (nd - 1) / 2, hist, bc);
+        if (threadIdx.x == 0) {
+            const double nrm = (double)rsqrt_magic((float)((double)__uint_as_float(mk) / kLn2));
+            s_n2[k] = nrm * nrm;
+        }
+        __syncthreads();
+    }
+    // summed power of every harmonic at (r, z)
+    auto summed = [&](double r, double z) {
+        double p = 0.0;
+        for (int k = 1; k <= H; k++) p += s_n2[k - 1] * warp_power(X, nb, r * k / H, z * k / H, lane);
+        return p;
+    };
+    if (threadIdx.x == 0) {
+        s_best[0] = cand.r;
+        s_best[1] = cand.z;
+    }
+    __syncthreads();
+    if (a.refine) {
+        const double dr[3] = {0.25, 1.0 / 16, 1.0 / 64}, dz[3] = {1.0, 0.25, 1.0 / 16};
+        for (int lv = 0; lv < 3; lv++) {
+            const double r0 = s_best[0], z0 = s_best[1];
+            for (int g = warp; g < 25; g += kOptWarps) {
+                const double p = summed(r0 + (g / 5 - 2) * dr[lv], z0 + (g % 5 - 2) * dz[lv]);
+                if (lane == 0) s_pow[g] = p;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int bg = 12;  // the centre unless something is strictly larger
+                for (int g = 0; g < 25; g++)
+                    if (s_pow[g] > s_pow[bg]) bg = g;
+                s_best[0] = r0 + (bg / 5 - 2) * dr[lv];
+                s_best[1] = z0 + (bg % 5 - 2) * dz[lv];
+            }
+            __syncthreads();
+        }
+    }
+    // the harmonics' powers at the final position (warp k % warps)
+    const double r = s_best[0], z = s_best[1];
+    __shared__ double s_h[kMaxHarm];
+    for (int k = 1 + warp; k <= H; k += kOptWarps) {
+        const double p = s_n2[k - 1] * warp_power(X, nb, r * k / H, z * k / H, lane);
+        if (lane == 0) s_h[k - 1] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        OptOut o;
+        o.r = r;
+        o.z = z;
+        double sum = 0.0;
+        for (int k = 0; k < kMaxHarm; k++) {
+            o.harm[k] = k < H ? (float)s_h[k] : 0.f;
+            if (k < H) sum += s_h[k];
+        }
+        o.power = sum;
+        a.out[ci] = o;
+    }
+}
+
+int launch_optimize(const OptArgs& a, cudaStream_t st) {
+    if (a.n <= 0) return 0;
+    const size_t smem = sizeof(uint32_t) * (size_t)a.maxdata;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_optimize, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    k_optimize<<<a.n, 32 * kOptWarps, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace accel

@@ -23,7 +23,8 @@ struct WhitenPlanDev {
 };
 
 struct TrialBuf {
-    long long n = 0;
+    long long n = 0;            // allocated samples
+    long long numbins = 0;      // whitened bins of the last search
     float* series = nullptr;
     float2* spec = nullptr;
 };
@@ -34,6 +35,7 @@ using namespace accel;  // internal header: the context is written in the librar
 
 struct accel_ctx {
     accel_config cfg{};
+    int last_trials = 0;        // trials of the last accel_search
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;

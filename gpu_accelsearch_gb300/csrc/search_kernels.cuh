@@ -26,7 +26,6 @@
 
 namespace accel {
 
-constexpr double kLn2 = 0.693147180559945309417232121458;
 
 
 // ------------------------------------------------------------------ prep

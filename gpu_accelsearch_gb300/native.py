@@ -61,6 +61,12 @@ class Tuning(C.Structure):
                 ("reserved", C.c_int * 2)]
 
 
+class Optimized(C.Structure):
+    _fields_ = [("cand", Candidate), ("r_grid", C.c_double), ("z_grid", C.c_double),
+                ("harm_power", C.c_float * 16), ("f", C.c_double), ("fdot", C.c_double),
+                ("period", C.c_double), ("pdot", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 6),
                 ("kind_ms", C.c_double * 6), ("segments", C.c_longlong),
@@ -106,6 +112,11 @@ SIGNATURES = {
     "accel_sift_candidates": (C.c_int, [C.POINTER(Candidate), C.c_longlong, C.c_double, C.c_int,
                                         C.c_double, C.POINTER(Candidate), C.c_longlong,
                                         C.POINTER(C.c_longlong)]),
+    "accel_optimize_candidates": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(C.c_longlong),
+                                            C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+                                            C.POINTER(Candidate), C.c_longlong,
+                                            C.c_int, C.POINTER(Optimized)]),
+    "accel_trial_spectrum": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(C.c_longlong)]),
     "accel_whiten": (C.c_int, [_vp, _vp, _ll]),
     "accel_rfft": (C.c_int, [_vp, _vp, _ll, _vp]),
     "accel_prepare_segments": (C.c_int, [_vp, _vp, _ll, _llp, C.c_int, _vp]),

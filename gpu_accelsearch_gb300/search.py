@@ -77,6 +77,12 @@ def sift_candidates(cands: np.ndarray, min_dr: float = 15.0, maxharm: int = 8,
     return _from_native(dst, m.value)
 
 
+OPT_DTYPE = np.dtype([("trial", "i4"), ("step", "i4"), ("r", "f8"), ("z", "f8"), ("numharm", "i4"),
+                      ("power", "f4"), ("sigma", "f4"), ("r_grid", "f8"), ("z_grid", "f8"),
+                      ("harm_power", "f4", (16,)), ("f", "f8"), ("fdot", "f8"), ("period", "f8"),
+                      ("pdot", "f8")])
+
+
 def first_bin(nsamples: int, dt: float) -> int:
     return N.lib().accel_first_bin(nsamples, dt)
 
@@ -275,6 +281,40 @@ class AccelSearch:
         nc = C.c_longlong()
         N.check(N.lib().accel_search_spectra(self._h, n, ptrs, nb, rl, C.byref(nc)))
         return nc.value
+
+    def trial_spectrum(self, trial: int):
+        """(device address, numbins) of trial's whitened spectrum from the last search."""
+        p = C.c_void_p()
+        nb = C.c_longlong()
+        N.check(N.lib().accel_trial_spectrum(self._h, int(trial), C.byref(p), C.byref(nb)))
+        return p.value, nb.value
+
+    def optimize(self, cands: np.ndarray, rlo, tobs, spectra=None, refine: bool = True) -> np.ndarray:
+        """accel_optimize_candidates.  spectra: [(device address, numbins)] per
+        trial (default: the whitened spectra of the last search); rlo and
+        tobs: the first bin searched and the observation time (s) of every
+        trial (or one value for all)."""
+        n = len(cands)
+        if spectra is None:
+            nt = int(cands["trial"].max()) + 1 if n else 1
+            spectra = [self.trial_spectrum(t) for t in range(nt)]
+        nt = len(spectra)
+        per = lambda v: list(v) if isinstance(v, (list, tuple, np.ndarray)) else [v] * nt
+        ptrs = (C.c_void_p * nt)(*[int(p) for p, _ in spectra])
+        nbs = (C.c_longlong * nt)(*[int(b) for _, b in spectra])
+        rl = (C.c_longlong * nt)(*[int(x) for x in per(rlo)])
+        tob = (C.c_double * nt)(*[float(x) for x in per(tobs)])
+        src = _to_native(cands)
+        dst = (N.Optimized * max(n, 1))()
+        N.check(N.lib().accel_optimize_candidates(self._h, nt, ptrs, nbs, rl, tob, src, n, int(refine),
+                                                  dst))
+        out = np.zeros(n, OPT_DTYPE)
+        for k in range(n):
+            o = dst[k]
+            c = o.cand
+            out[k] = (c.trial, c.step, c.r, c.z, c.numharm, c.power, c.sigma, o.r_grid, o.z_grid,
+                      tuple(o.harm_power), o.f, o.fdot, o.period, o.pdot)
+        return out
 
     def candidates(self) -> np.ndarray:
         L = N.lib()

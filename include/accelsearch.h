@@ -189,6 +189,36 @@ int  accel_candidates(accel_ctx *ctx, accel_candidate *out, long long cap, long 
 int  accel_sift_candidates(const accel_candidate *in, long long n, double min_dr, int maxharm,
                            double harm_dr, accel_candidate *out, long long cap, long long *nout);
 
+/* A refined candidate with the properties of its fundamental. */
+typedef struct accel_optimized {
+    accel_candidate cand;   /* r, z, power and sigma at the refined position  */
+    double r_grid, z_grid;  /* the position it started from                   */
+    float harm_power[16];   /* power of harmonic k r/numharm, k z/numharm     */
+    double f, fdot;         /* r / T (Hz) and z / T^2 (Hz/s), T = tobs        */
+    double period, pdot;    /* 1 / f (s) and -fdot / f^2                      */
+} accel_optimized;
+
+/* Candidate refinement and properties (the reference's optimizeCandidates
+ * and calculateProperties stubs, bpd_candidates.cu:24-33).  For each
+ * candidate, on the whitened spectrum of its trial: the summed power of its
+ * numharm harmonics (k r/numharm, k z/numharm; each the plane kernels'
+ * correlation |sum_j X[j] conj(F(r - j - z/2; z))|^2 over 2 hw(z) bins,
+ * F the response of generate_z_response, bpd_subharmonics.cu:146-226,
+ * scaled by the segment normalisation the search applied to that harmonic
+ * in the candidate's step) is maximised over three nested 5 x 5 grids
+ * (steps 1/4, 1/16, 1/64 bins in r and 1, 1/4, 1/16 in z); refine = 0 only
+ * evaluates at the given position.  wspec_dev[t], numbins[t], rlo[t] (the
+ * first bin searched) and tobs[t] (seconds) describe trial t.  numharm of
+ * every candidate must be one of this context's stages. */
+int  accel_optimize_candidates(accel_ctx *ctx, int ntrials, const accel_complex *const *wspec_dev,
+                               const long long *numbins, const long long *rlo, const double *tobs,
+                               const accel_candidate *in, long long n, int refine,
+                               accel_optimized *out);
+/* The whitened spectrum of trial t of the last accel_search, resident on the
+ * device until the next search (for accel_optimize_candidates). */
+int  accel_trial_spectrum(accel_ctx *ctx, int trial, const accel_complex **spec_dev,
+                          long long *numbins);
+
 /* ------------------------------------------------------------ stage calls */
 /* Whitening in place (deredden, bpd_noise.c:12-92). */
 int  accel_whiten(accel_ctx *ctx, accel_complex *spec_dev, long long numbins);

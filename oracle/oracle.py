@@ -276,3 +276,77 @@ def sift(cands, min_dr=15.0, maxharm=8, harm_dr=1.0):
                 final.append(c)
         out.extend(final)
     return out
+
+
+def harmonic_power(wspec, r, z):
+    """|sum_j X[j] conj(F(r - j - z/2; z))|^2 over the 2 hw(z) bins j in
+    [ceil(r - hw), ceil(r + hw)): the plane kernels' correlation at any
+    (r, z), with F from the restated generate_z_response (numbetween 1,
+    offset chosen so that its samples fall on x = r - j - z/2)."""
+    import math
+    hw = z_halfwidth(z)
+    j0 = math.ceil(r - hw)
+    # samples x = r - j - z/2 for j = j0 .. j0 + 2hw - 1 are 2hw consecutive
+    # elements of a 2hw+2 point response with its offset in [0, 1) (the range
+    # the reference's routine is written for), starting at element s
+    d = r - j0
+    off = d - math.floor(d)
+    s = int(round(off + hw + 1 - d))
+    resp = z_response(z, 2 * hw + 2, roffset=off, numbetween=1)[s: s + 2 * hw]
+    resp = resp.astype(np.complex128)
+    j = np.arange(j0, j0 + 2 * hw)
+    ok = (j >= 0) & (j < len(wspec))
+    x = np.zeros(2 * hw, np.complex128)
+    x[ok] = wspec[j[ok]]
+    a = np.sum(x * np.conj(resp))
+    return float(a.real * a.real + a.imag * a.imag)
+
+
+def step_norms(wspec, zmax, bank_numharm, uselen, rlo, step, numharm):
+    """Squared segment normalisation of harmonics k/numharm (k = 1..numharm)
+    in overlap-save step `step` of a trial whose first bin is rlo: the
+    magic rsqrt of the lower median of |X|^2 over the segment's numdata bins
+    divided by ln 2 (bpd_search.cu:130-184)."""
+    from math import gcd, ceil, log
+    geom = bank_geometry(zmax, bank_numharm, uselen)
+    startr = rlo + step * (uselen // 2)
+    out = []
+    for k in range(1, numharm + 1):
+        g = gcd(k, numharm)
+        p, q = k // g, numharm // g
+        row = [rw for rw in geom if int(rw[0]) == p and int(rw[1]) == q][0]
+        hw0, fftlen = int(row[5]), int(row[4])
+        rl, rh, _, _ = step_ffdot(p, q, zmax, uselen, float(startr), startr + uselen // 2 - 0.5)
+        lobin = rl - hw0
+        numdata = min(int(ceil(rh)) + hw0 - lobin + 1, fftlen // 2)
+        idx = np.arange(lobin, lobin + numdata)
+        v = np.zeros(numdata, np.complex64)
+        ok = (idx >= 0) & (idx < len(wspec))
+        v[ok] = wspec[idx[ok]]
+        pw = (v.real * v.real + v.imag * v.imag).astype(np.float32)
+        nrm = rsqrt_magic(float(np.float64(lower_median(pw)) / log(2.0)))
+        out.append(float(nrm) * float(nrm))
+    return out
+
+
+def optimize(wspec, r, z, numharm, norms, refine=True):
+    """Candidate refinement restated: the summed power of harmonics
+    k r/numharm, k z/numharm (k = 1..numharm; harmonic k scaled by norms[k-1])
+    maximised over three nested 5 x 5 grids (steps 1/4, 1/16, 1/64 in r;
+    1, 1/4, 1/16 in z), the centre kept unless a point is strictly larger.
+    Returns (r, z, power, powers per harmonic)."""
+    def summed(rr, zz):
+        return sum(norms[k - 1] * harmonic_power(wspec, rr * k / numharm, zz * k / numharm)
+                   for k in range(1, numharm + 1))
+    if refine:
+        for dr, dz in ((0.25, 1.0), (1 / 16, 0.25), (1 / 64, 1 / 16)):
+            pts = [(r + (g // 5 - 2) * dr, z + (g % 5 - 2) * dz) for g in range(25)]
+            p = [summed(a, b) for a, b in pts]
+            best = 12
+            for g in range(25):
+                if p[g] > p[best]:
+                    best = g
+            r, z = pts[best]
+    hp = [norms[k - 1] * harmonic_power(wspec, r * k / numharm, z * k / numharm)
+          for k in range(1, numharm + 1)]
+    return r, z, sum(hp), hp
