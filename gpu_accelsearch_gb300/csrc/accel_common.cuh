@@ -25,6 +25,19 @@ constexpr int kDz = 2;              // f-dot step (bpd_common.h:33)
 constexpr double kLn2 = 0.693147180559945309417232121458;  // median -> mean of an exponential
 constexpr int kFintBins = 16;       // NUMFINTBINS (bpd_common.h:45)
 constexpr int kTwN = 8192;          // twiddle table length (max FFT points)
+// Behind the kTwN-entry table: for every later-pass length NR of the
+// shared-memory FFT, the base twiddles W^k, W^2k, W^4k, W^8k of pass index k
+// (W = exp(2 pi i / NR)) side by side, four float2 per k, so that a thread
+// fetches its pass's base twiddles with two 16-byte loads from consecutive
+// memory instead of four scattered ones.  Sections: NR = 64, 128, 256 (16
+// entries each), 512, 1024, 2048, 4096 (256 entries each).
+ACCEL_HD constexpr int tw_pack_entries(int NR) { return NR <= 256 ? 16 : 256; }
+ACCEL_HD constexpr int tw_pack_off(int NR) {  // in float2, from the start of the packed part
+    return NR == 64 ? 0 : NR == 128 ? 64 : NR == 256 ? 128 : NR == 512 ? 192 : NR == 1024 ? 1216
+         : NR == 2048 ? 2240 : 3264;           // NR == 4096
+}
+constexpr int kTwPacked = 4288;     // float2 of the packed sections (3264 + 4 * 256)
+constexpr int kTwTotal = kTwN + kTwPacked;
 constexpr int kMinM = 64;           // smallest half-length FFT
 constexpr int kMaxM = 8192;         // largest half-length FFT (L <= 16384)
 

@@ -771,7 +771,7 @@ int accel_create(const accel_config* cfg, accel_ctx** out) {
         c->own_stream = true;
     }
     if (!rc) {
-        cudaError_t e = cudaMalloc(&c->tw, sizeof(float2) * kTwN);
+        cudaError_t e = cudaMalloc(&c->tw, sizeof(float2) * kTwTotal);
         if (e != cudaSuccess) rc = set_err(ACCEL_ERR_NOMEM, "twiddles: %s", cudaGetErrorString(e));
         else if (launch_twiddles(c->tw, c->stream) != 0) rc = set_err(ACCEL_ERR_CUDA, "twiddle launch");
     }

@@ -246,17 +246,28 @@ __global__ void k_fold_to_half(const BankHarmDev* __restrict__ hd, int nh) {
     }
 }
 
+// Entry i of the twiddle buffer: the table W^m (m < kTwN), then the packed
+// per-pass sections (accel_common.cuh), each a copy of table entry m.
 __global__ void k_twiddles(float2* tw) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < kTwN) {
-        double s, c;
-        sincospi(2.0 * m / kTwN, &s, &c);
-        tw[m] = make_float2((float)c, (float)s);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kTwTotal) return;
+    int m = i;
+    if (i >= kTwN) {
+        const int p = i - kTwN;
+        const int nrs[7] = {64, 128, 256, 512, 1024, 2048, 4096};
+        int NR = 64;
+        for (int j = 0; j < 7; j++)
+            if (p >= tw_pack_off(nrs[j])) NR = nrs[j];
+        const int q = p - tw_pack_off(NR), k = q >> 2, slot = q & 3;
+        m = ((1 << slot) * k * (kTwN / NR)) & (kTwN - 1);
     }
+    double s, c;
+    sincospi(2.0 * m / kTwN, &s, &c);
+    tw[i] = make_float2((float)c, (float)s);
 }
 
 int launch_twiddles(float2* tw, cudaStream_t st) {
-    k_twiddles<<<(kTwN + 255) / 256, 256, 0, st>>>(tw);
+    k_twiddles<<<(kTwTotal + 255) / 256, 256, 0, st>>>(tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

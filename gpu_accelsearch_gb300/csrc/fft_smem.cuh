@@ -115,20 +115,46 @@ template <int DIR> __device__ __forceinline__ float2 twid(const float2* __restri
     return DIR > 0 ? w : make_float2(w.x, -w.y);
 }
 
+// The base twiddles W^k, W^2k, W^4k, W^8k (W = exp(DIR 2 pi i / NR)) of
+// pass index k: from the packed section of NR (two 16-byte loads of
+// consecutive memory) or, for NR = kTwN, from the table itself.
+struct Tw16 {
+    float2 w1, w2, w4, w8;
+};
+template <int DIR>
+__device__ __forceinline__ Tw16 load_tw16(const float2* __restrict__ tw, int k, int NR) {
+    Tw16 r;
+    if (NR == kTwN) {
+        r.w1 = twid<DIR>(tw, k);
+        r.w2 = twid<DIR>(tw, (2 * k) & (kTwN - 1));
+        r.w4 = twid<DIR>(tw, (4 * k) & (kTwN - 1));
+        r.w8 = twid<DIR>(tw, (8 * k) & (kTwN - 1));
+        return r;
+    }
+    const float4* p = reinterpret_cast<const float4*>(tw + kTwN + tw_pack_off(NR)) + 2 * k;
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    const float sg = DIR > 0 ? 1.f : -1.f;
+    r.w1 = make_float2(a.x, sg * a.y);
+    r.w2 = make_float2(a.z, sg * a.w);
+    r.w4 = make_float2(b.x, sg * b.y);
+    r.w8 = make_float2(b.z, sg * b.w);
+    return r;
+}
+
 // v[nb][r] *= W^{r k} with W = exp(DIR 2 pi i / NR), for every transform nb.
-// Table lookups for r = 1, 2, 4; the rest are one product away.
+// Base powers from load_tw16; the rest are one product away.
 template <int R, int DIR, int NB>
 __device__ __forceinline__ void apply_twiddles(float2 (&v)[NB][R], const float2* __restrict__ tw, int k,
                                                int NR) {
     static_assert(R <= 8, "radix-16 passes use apply_tw16");
-    const int base = k * (kTwN / NR);
+    const Tw16 b = load_tw16<DIR>(tw, k, NR);
     float2 w[R];
-    w[1] = twid<DIR>(tw, base);
+    w[1] = b.w1;
     if constexpr (R >= 4) {
-        w[2] = twid<DIR>(tw, 2 * base);
+        w[2] = b.w2;
         w[3] = cmul(w[2], w[1]);
         if constexpr (R >= 8) {
-            w[4] = twid<DIR>(tw, 4 * base);
+            w[4] = b.w4;
             w[5] = cmul(w[4], w[1]);
             w[6] = cmul(w[4], w[2]);
             w[7] = cmul(w[4], w[3]);
@@ -140,21 +166,6 @@ __device__ __forceinline__ void apply_twiddles(float2 (&v)[NB][R], const float2*
         for (int r = 1; r < R; r++) v[nb][r] = cmul(v[nb][r], w[r]);
 }
 
-// Base twiddles W^k, W^2k, W^4k, W^8k of one radix-16 pass, loaded ahead of
-// time so that the table lookups are off the pass's critical path.
-struct Tw16 {
-    float2 w1, w2, w4, w8;
-};
-template <int DIR>
-__device__ __forceinline__ Tw16 load_tw16(const float2* __restrict__ tw, int k, int NR) {
-    const int base = k * (kTwN / NR);
-    Tw16 r;
-    r.w1 = twid<DIR>(tw, base);
-    r.w2 = twid<DIR>(tw, 2 * base);
-    r.w4 = twid<DIR>(tw, 4 * base);
-    r.w8 = twid<DIR>(tw, 8 * base);
-    return r;
-}
 template <int NB>
 __device__ __forceinline__ void apply_tw16(float2 (&v)[NB][16], const Tw16& p) {
     float2 w[16];
