@@ -36,7 +36,11 @@ ACCEL_HD constexpr int tw_pack_off(int NR) {  // in float2, from the start of th
     return NR == 64 ? 0 : NR == 128 ? 64 : NR == 256 ? 128 : NR == 512 ? 192 : NR == 1024 ? 1216
          : NR == 2048 ? 2240 : 3264;           // NR == 4096
 }
-constexpr int kTwPacked = 4288;     // float2 of the packed sections (3264 + 4 * 256)
+// Then, for the radix-16 pass with NR = 256 (16 distinct k, so one warp's
+// loads of a slot fall in one 128-byte line), all fifteen powers W^jk,
+// j = 1..15, slot-major: entry (j - 1) * 16 + k.
+constexpr int kTwFull256 = 4288;    // offset of that section in the packed part
+constexpr int kTwPacked = 4288 + 15 * 16;
 constexpr int kTwTotal = kTwN + kTwPacked;
 constexpr int kMinM = 64;           // smallest half-length FFT
 constexpr int kMaxM = 8192;         // largest half-length FFT (L <= 16384)

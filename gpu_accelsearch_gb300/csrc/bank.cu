@@ -252,7 +252,10 @@ __global__ void k_twiddles(float2* tw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kTwTotal) return;
     int m = i;
-    if (i >= kTwN) {
+    if (i >= kTwN + kTwFull256) {
+        const int q = i - kTwN - kTwFull256, j = q / 16 + 1, k = q % 16;
+        m = (j * k * (kTwN / 256)) & (kTwN - 1);
+    } else if (i >= kTwN) {
         const int p = i - kTwN;
         const int nrs[7] = {64, 128, 256, 512, 1024, 2048, 4096};
         int NR = 64;

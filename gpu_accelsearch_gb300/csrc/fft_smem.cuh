@@ -166,6 +166,19 @@ __device__ __forceinline__ void apply_twiddles(float2 (&v)[NB][R], const float2*
         for (int r = 1; r < R; r++) v[nb][r] = cmul(v[nb][r], w[r]);
 }
 
+// v[nb][r] *= W^{rk} for the radix-16 pass with NR = 256, every power from
+// its own table entry (no products).
+template <int DIR, int NB>
+__device__ __forceinline__ void apply_tw16_full256(float2 (&v)[NB][16], const float2* __restrict__ tw, int k) {
+    const float2* f = tw + kTwN + kTwFull256 + k;
+#pragma unroll
+    for (int r = 1; r < 16; r++) {
+        const float2 w = twid<DIR>(f, (r - 1) * 16);
+#pragma unroll
+        for (int nb = 0; nb < NB; nb++) v[nb][r] = cmul(v[nb][r], w);
+    }
+}
+
 template <int NB>
 __device__ __forceinline__ void apply_tw16(float2 (&v)[NB][16], const Tw16& p) {
     float2 w[16];
@@ -234,7 +247,9 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
             for (int r = 0; r < R; r++) v[nb][r] = a[nb][q + r * Q];
         if constexpr (NS > 1) {
             // each twiddle is formed once and applied to every transform
-            if constexpr (R == 16) {
+            if constexpr (R == 16 && NS == 16) {
+                apply_tw16_full256<DIR, NB>(v, tw, k);
+            } else if constexpr (R == 16) {
                 if (pre) apply_tw16<NB>(v, *pre);
                 else apply_tw16<NB>(v, load_tw16<DIR>(tw, k, NS * R));
             } else {
@@ -284,26 +299,22 @@ __device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const f
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, 8, 16, false, true, DIR, NB>(a, sm, tw, t);
     } else if constexpr (M == 256) {
-        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, true, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 16, false, true, DIR, NB>(a, sm, tw, t);
     } else if constexpr (M == 512 || M == 1024 || M == 2048) {
         constexpr int RL = M / 256;
-        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, RL, 256, false, true, DIR, NB>(a, sm, tw, t);
     } else if constexpr (M == 4096) {
-        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, 16, 256, false, true, DIR, NB>(a, sm, tw, t, &p2);
     } else {  // 8192
-        const Tw16 p1 = load_tw16<DIR>(tw, t & 15, 256);
         const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
         fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t, &p1);
+        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
         fft_pass<M, 16, 256, false, false, DIR, NB>(a, sm, tw, t, &p2);
         fft_pass<M, 2, 4096, false, true, DIR, NB>(a, sm, tw, t);
     }
