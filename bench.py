@@ -392,7 +392,7 @@ def run_ours(args):
     tuned = None
     if args.fftlen == 0 or args.chunk == 0 or args.split < 0:
         fl = (4096, 8192, 16384) if args.fftlen == 0 else (args.fftlen,)
-        kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=96, device=local)
+        kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=1100, device=local)
         tuned = {"fftlen": kw["fftlen"], "chunk_segments": tun["chunk_segments"],
                  "plane_split": tun["plane_split"], "fused_sum": tun["fused_sum"],
                  "sample_cells_per_s": rate}

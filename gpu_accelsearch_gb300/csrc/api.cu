@@ -342,7 +342,7 @@ int alloc_work(accel_ctx* c) {
     long long plane_bytes = c->pstride * 4;
     int chunk = c->cfg.chunk_segments;
     if (chunk <= 0) {
-        chunk = (int)std::max(1LL, std::min(256LL, (2LL << 30) / plane_bytes));
+        chunk = (int)std::max(1LL, std::min(512LL, (8LL << 30) / plane_bytes));  // up to 8 GB of planes
     }
     c->chunk = chunk;
     CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * chunk));

@@ -49,7 +49,8 @@ extern "C" int accel_autotune(const accel_config* base, const int* fftlens, int 
     if (!base || !fftlens || nlens <= 0 || steps <= 0 || !best_cfg || !best_tuning)
         return set_error(ACCEL_ERR_INVALID, "accel_autotune: bad argument");
     double best = -1.0;
-    const int chunks[] = {8, 16, 32, 64, 128};
+    const int chunks[] = {16, 32, 64, 128, 256, 512};
+    constexpr int kChunks = 6;
     for (int li = 0; li < nlens; li++) {
         accel_config cfg = *base;
         cfg.fftlen = fftlens[li];
@@ -79,7 +80,8 @@ extern "C" int accel_autotune(const accel_config* base, const int* fftlens, int 
         if (!rc) rc = accel_whiten(ctx, reinterpret_cast<accel_complex*>(spec), numbins);
         const accel_complex* sp = reinterpret_cast<const accel_complex*>(spec);
         for (int combo = 0; combo < 4 && !rc; combo++) {
-            for (int ci = 0; ci < 5 && !rc; ci++) {
+            for (int ci = 0; ci < kChunks && !rc; ci++) {
+                if (ci > 0 && chunks[ci] > steps) break;  // the sample would fit in one group anyway
                 accel_tuning t{};
                 t.chunk_segments = chunks[ci];
                 t.plane_split = combo & 1;
