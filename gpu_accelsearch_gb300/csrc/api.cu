@@ -10,6 +10,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -557,8 +558,11 @@ struct SegSpan {
     std::vector<int> trial, step;
 };
 
+// prepare(t), when given, is called on the main stream before the first
+// launch group that holds a segment of trial t (trials in order), so that a
+// trial's transform and whitening are issued just ahead of its search.
 int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* numbins,
-               const long long* rlo) {
+               const long long* rlo, const std::function<int(int)>& prepare) {
     long long total = 0;
     const long long half = (unsigned short)(c->uselen / 2);
     std::vector<long long> nsteps(ntrials);
@@ -590,8 +594,18 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         CK(cudaEventRecord(c->ev_fork, c->stream));
         CK(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
     }
+    int prepared = 0;  // trials [0, prepared) have been prepared
+    auto prepare_upto = [&](int last) -> int {
+        for (; prepare && prepared <= last && prepared < ntrials; prepared++) {
+            const int r = prepare(prepared);
+            if (r) return r;
+        }
+        return ACCEL_OK;
+    };
     for (long long g = 0, k = 0; g < total; g += c->chunk, k++) {
         int n = (int)std::min<long long>(c->chunk, total - g);
+        rc = prepare_upto(c->h_segs[g + n - 1].trial);
+        if (rc) return rc;
         if (!overlap) {
             rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true,
                            c->fused_sum != 0);
@@ -611,6 +625,8 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         if (rc) return rc;
         CK(cudaEventRecord(c->ev_sum[b], c->stream2));
     }
+    rc = prepare_upto(ntrials - 1);
+    if (rc) return rc;
     if (overlap) {
         // join: the main stream continues after the last sum
         CK(cudaEventRecord(c->ev_fork, c->stream2));
@@ -691,6 +707,8 @@ void free_ctx(accel_ctx* c) {
     cudaFree(c->planes);
     cudaFree(c->planes2);
     if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (cudaEvent_t e : c->copy_ev) cudaEventDestroy(e);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     for (int b = 0; b < 2; b++) {
         if (c->ev_plane[b]) cudaEventDestroy(c->ev_plane[b]);
@@ -981,7 +999,18 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
     int rc = ensure_device(c);
     if (rc) return rc;
     if ((int)c->trials.size() < ntrials) c->trials.resize(ntrials);
+    if (!on_device) {
+        // the series are copied on their own stream, so that trial i+1 lands
+        // while trial i is transformed and whitened
+        if (!c->copy_stream) CK(cudaStreamCreate(&c->copy_stream));
+        while ((int)c->copy_ev.size() < ntrials) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            c->copy_ev.push_back(e);
+        }
+    }
     CK(cudaEventRecord(c->ev_begin, c->stream));
+    if (!on_device) CK(cudaStreamWaitEvent(c->copy_stream, c->ev_begin, 0));
     std::vector<float2*> specs(ntrials);
     std::vector<long long> nb(ntrials), rlo(ntrials);
     for (int i = 0; i < ntrials; i++) {
@@ -990,6 +1019,8 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
             return set_err(ACCEL_ERR_INVALID, "trial %d: sample count %lld must be even and >= 4", i, n);
         TrialBuf& t = c->trials[i];
         if (t.n < n) {
+            CK(cudaStreamSynchronize(c->stream));
+            if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
             cudaFree(t.series);
             cudaFree(t.spec);
             t.series = nullptr;
@@ -999,22 +1030,33 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
             CK(cudaMalloc(&t.spec, sizeof(float2) * (n / 2 + 1)));
             t.n = n;
         }
+        if (!on_device) {
+            CK(cudaMemcpyAsync(t.series, series[i], sizeof(float) * n, cudaMemcpyHostToDevice, c->copy_stream));
+            CK(cudaEventRecord(c->copy_ev[i], c->copy_stream));
+        }
+    }
+    for (int i = 0; i < ntrials; i++) {
+        TrialBuf& t = c->trials[i];
+        specs[i] = t.spec;
+        nb[i] = nsamples[i] / 2;
+        t.numbins = nsamples[i] / 2;
+        rlo[i] = accel_first_bin(nsamples[i], dt[i]);
+    }
+    // a trial's R2C and whitening are issued just before the first launch
+    // group that needs it, so the copies of later trials overlap the search
+    auto prepare = [&](int i) -> int {
+        TrialBuf& t = c->trials[i];
         const float* src = series[i];
         if (!on_device) {
-            CK(cudaMemcpyAsync(t.series, series[i], sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaStreamWaitEvent(c->stream, c->copy_ev[i], 0));
             src = t.series;
         }
-        rc = do_rfft(c, src, n, t.spec);
-        if (rc) return rc;
-        rc = do_whiten(c, t.spec, (unsigned)(n / 2));
-        if (rc) return rc;
-        specs[i] = t.spec;
-        nb[i] = n / 2;
-        t.numbins = n / 2;
-        rlo[i] = accel_first_bin(n, dt[i]);
-    }
+        int r = do_rfft(c, src, nsamples[i], t.spec);
+        if (!r) r = do_whiten(c, t.spec, (unsigned)(nsamples[i] / 2));
+        return r;
+    };
     c->last_trials = ntrials;
-    rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data());
+    rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data(), prepare);
     if (ncand) *ncand = (long long)c->last_raw;
     return rc;
 }
@@ -1028,7 +1070,7 @@ int accel_search_spectra(accel_ctx* c, int ntrials, const accel_complex* const* 
     CK(cudaEventRecord(c->ev_begin, c->stream));
     std::vector<float2*> specs(ntrials);
     for (int i = 0; i < ntrials; i++) specs[i] = (float2*)wspec[i];
-    rc = run_search(c, ntrials, specs.data(), numbins, rlo);
+    rc = run_search(c, ntrials, specs.data(), numbins, rlo, nullptr);
     if (ncand) *ncand = (long long)c->last_raw;
     return rc;
 }

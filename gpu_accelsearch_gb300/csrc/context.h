@@ -61,6 +61,8 @@ struct accel_ctx {
     int fused_sum = 0;
     int overlap = 1;          // sum of group k on stream2 while group k+1 is transformed
     cudaStream_t stream2 = nullptr;
+    cudaStream_t copy_stream = nullptr;       // host-to-device copies of the series
+    std::vector<cudaEvent_t> copy_ev;         // one per trial: its series has landed
     float* planes2 = nullptr; // second plane buffer for the overlap
     cudaEvent_t ev_fork = nullptr, ev_plane[2] = {nullptr, nullptr}, ev_sum[2] = {nullptr, nullptr};
     bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
