@@ -449,9 +449,12 @@ def run_ours(args):
         torch.cuda.synchronize()
         s.reset_stats()
         nc = 0
+        clk2 = Clocks(local)
+        clk2.start()
         for _ in range(args.steps):
             nc = s.search_ptrs(hptrs, lengths, DT, on_device=False)
         torch.cuda.synchronize()
+        clocks_e2e = clk2.stop()
         el2 = s.stats()["search_ms"] / 1e3
         barrier()
         el2_t = torch.tensor([el2], device="cuda")
@@ -459,7 +462,7 @@ def run_ours(args):
             dist.all_reduce(el2_t, op=dist.ReduceOp.MAX)
         e2e = {"value": cells * args.steps * world / float(el2_t.item()), "unit": "cells/s",
                "h2d_bytes_per_step": int(sum(lengths) * 4),
-               "d2h_bytes_per_step": int(8 + 16 * nc)}
+               "d2h_bytes_per_step": int(8 + 16 * nc), "clocks": clocks_e2e}
 
     # ---- plain per-trial path: one 2^22 trial, one step per launch group
     plain = None
