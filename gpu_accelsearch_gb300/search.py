@@ -48,20 +48,32 @@ CAND_DTYPE = np.dtype([("trial", "i4"), ("step", "i4"), ("r", "f8"), ("z", "f8")
                        ("numharm", "i4"), ("power", "f4"), ("sigma", "f4")])
 
 
+def _native_dtype():
+    """numpy view of N.Candidate (same offsets and size)."""
+    return np.dtype({"names": ["trial", "step", "r", "z", "numharm", "power", "sigma"],
+                     "formats": ["i4", "i4", "f8", "f8", "i4", "f4", "f4"],
+                     "offsets": [N.Candidate.trial.offset, N.Candidate.step.offset,
+                                 N.Candidate.r.offset, N.Candidate.z.offset,
+                                 N.Candidate.numharm.offset, N.Candidate.power.offset,
+                                 N.Candidate.sigma.offset],
+                     "itemsize": C.sizeof(N.Candidate)})
+
+
 def _to_native(cands: np.ndarray):
     buf = (N.Candidate * max(len(cands), 1))()
-    for k, c in enumerate(cands):
-        buf[k].trial, buf[k].step = int(c["trial"]), int(c["step"])
-        buf[k].r, buf[k].z = float(c["r"]), float(c["z"])
-        buf[k].numharm, buf[k].power, buf[k].sigma = int(c["numharm"]), float(c["power"]), float(c["sigma"])
+    if len(cands):
+        view = np.frombuffer(buf, dtype=_native_dtype(), count=len(cands))
+        for f in CAND_DTYPE.names:
+            view[f] = cands[f]
     return buf
 
 
 def _from_native(buf, n: int) -> np.ndarray:
     out = np.zeros(n, CAND_DTYPE)
-    for k in range(n):
-        c = buf[k]
-        out[k] = (c.trial, c.step, c.r, c.z, c.numharm, c.power, c.sigma)
+    if n:
+        view = np.frombuffer(buf, dtype=_native_dtype(), count=n)
+        for f in CAND_DTYPE.names:
+            out[f] = view[f]
     return out
 
 
