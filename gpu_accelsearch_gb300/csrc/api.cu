@@ -1042,8 +1042,10 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
         t.numbins = nsamples[i] / 2;
         rlo[i] = accel_first_bin(nsamples[i], dt[i]);
     }
-    // a trial's R2C and whitening are issued just before the first launch
-    // group that needs it, so the copies of later trials overlap the search
+    // from host memory, a trial's R2C and whitening are issued just before
+    // the first launch group that needs it, so that the copies of later
+    // trials overlap the search; series already on the device are all
+    // prepared first
     auto prepare = [&](int i) -> int {
         TrialBuf& t = c->trials[i];
         const float* src = series[i];
@@ -1056,7 +1058,13 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
         return r;
     };
     c->last_trials = ntrials;
-    rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data(), prepare);
+    if (on_device) {
+        for (int i = 0; i < ntrials && !rc; i++) rc = prepare(i);
+        if (rc) return rc;
+        rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data(), nullptr);
+    } else {
+        rc = run_search(c, ntrials, specs.data(), nb.data(), rlo.data(), prepare);
+    }
     if (ncand) *ncand = (long long)c->last_raw;
     return rc;
 }
