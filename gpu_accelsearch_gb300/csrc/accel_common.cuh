@@ -127,6 +127,11 @@ __device__ __forceinline__ float rsqrt_magic(float x) {
     h = __fmul_rn(h, y);
     return __fmul_rn(y, __fsub_rn(1.5f, h));
 }
+// The normalisation factor 1/sqrt(x): the reference's approximation, or
+// (exact) IEEE single precision.
+__device__ __forceinline__ float rsqrt_norm(float x, int exact) {
+    return exact ? __fdiv_rn(1.0f, __fsqrt_rn(x)) : rsqrt_magic(x);
+}
 
 // |a|^2 as the reference host code evaluates it: x*x + y*y, two rounded
 // products and a rounded sum.

@@ -62,6 +62,7 @@ struct PrepArgs {
     const SegDesc* segs;
     float2* dbuf;           // [nseg][dstride]
     long long dstride;
+    int exact_rsqrt;        // IEEE 1/sqrt instead of the magic-constant one
 };
 
 struct PlaneArgs {
@@ -158,6 +159,7 @@ struct OptArgs {
     int n;
     int refine;                  // 0: evaluate at the given position only
     int maxdata;                 // largest numdata (shared-memory keys)
+    int exact_rsqrt;
 };
 
 // ---- launchers (return 0 or -1 after a launch error) ----
@@ -184,6 +186,6 @@ int set_error(int code, const char* fmt, ...);
 // whitening
 struct WhitenPlan;
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
-                  unsigned numbins, int maxlen, cudaStream_t st);
+                  unsigned numbins, int maxlen, cudaStream_t st, int exact_rsqrt = 0);
 
 }  // namespace accel

@@ -408,7 +408,8 @@ int do_whiten(accel_ctx* c, float2* spec, unsigned numbins) {
     int rc = whiten_plan(c, numbins, &w);
     if (rc) return rc;
     ProfScope ps(c, K_WHITEN, 2);
-    CKL(launch_whiten(w->d_start, w->d_len, w->nb, w->d_med, spec, numbins, w->maxlen, c->stream),
+    CKL(launch_whiten(w->d_start, w->d_len, w->nb, w->d_med, spec, numbins, w->maxlen, c->stream,
+                      c->cfg.exact_rsqrt),
         "whitening");
     return ACCEL_OK;
 }
@@ -470,6 +471,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         }
         pa.nh = k;
         pa.uselen = c->uselen;
+        pa.exact_rsqrt = c->cfg.exact_rsqrt;
         pa.segs = d_segs;
         pa.dbuf = dbuf;
         pa.dstride = c->dstride;

@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_optimize(const OptArgs a) {
         __syncthreads();
         const uint32_t mk = block_select_u32(okeys, nd, (nd - 1) / 2, hist, bc);
         if (threadIdx.x == 0) {
-            const double nrm = (double)rsqrt_magic((float)((double)__uint_as_float(mk) / kLn2));
+            const double nrm = (double)rsqrt_norm((float)((double)__uint_as_float(mk) / kLn2), a.exact_rsqrt);
             s_n2[k] = nrm * nrm;
         }
         __syncthreads();

@@ -80,6 +80,7 @@ extern "C" int accel_optimize_candidates(accel_ctx* c, int ntrials, const accel_
         a.n = (int)n;
         a.refine = refine != 0;
         a.maxdata = maxdata;
+        a.exact_rsqrt = c->cfg.exact_rsqrt;
         if (launch_optimize(a, c->stream) != 0) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaGetLastError();
     }

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(M / 16) k_prep(const PrepArgs a, const float2*
     }
     __syncthreads();
     const uint32_t mk = block_select_u32(keys, numdata, (numdata - 1) / 2, hist, bc);
-    if (t == 0) s_norm = rsqrt_magic((float)((double)__uint_as_float(mk) / kLn2));
+    if (t == 0) s_norm = rsqrt_norm((float)((double)__uint_as_float(mk) / kLn2), a.exact_rsqrt);
     __syncthreads();
     const float norm = s_norm;
 #pragma unroll

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_whiten_medians(const int* __restrict__ 
 __global__ void __launch_bounds__(256) k_whiten_scale(const int* __restrict__ bstart,
                                                       const int* __restrict__ blen,
                                                       const double* __restrict__ med, int nb,
-                                                      float2* spec, unsigned numbins) {
+                                                      float2* spec, unsigned numbins, int exact) {
     const int r = blockIdx.x;
     long long lo, hi;
     float mean_old, dslope;
@@ -67,11 +67,11 @@ __global__ void __launch_bounds__(256) k_whiten_scale(const int* __restrict__ bs
             dslope = 1.0f;
         }
     }
-    const float flat = rsqrt_magic(mean_old);
+    const float flat = rsqrt_norm(mean_old, exact);
     for (long long ind = lo + threadIdx.x; ind < hi; ind += blockDim.x) {
         float norm;
         if (r == 0) norm = flat;
-        else norm = rsqrt_magic(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))));
+        else norm = rsqrt_norm(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))), exact);
         float2 v = spec[ind];
         v.x = __fmul_rn(v.x, norm);
         v.y = __fmul_rn(v.y, norm);
@@ -169,7 +169,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_medians_warp(const
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_scale_warp(const int* __restrict__ bstart,
                                                                          const int* __restrict__ blen,
                                                                          const double* __restrict__ med, int nb,
-                                                                         float2* spec, unsigned numbins) {
+                                                                         float2* spec, unsigned numbins,
+                                                                         int exact) {
     const int r = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (r > nb) return;
     long long lo, hi;
@@ -196,11 +197,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_scale_warp(const i
             dslope = 1.0f;
         }
     }
-    const float flat = rsqrt_magic(mean_old);
+    const float flat = rsqrt_norm(mean_old, exact);
     for (long long ind = lo + lane; ind < hi; ind += 32) {
         float norm;
         if (r == 0) norm = flat;
-        else norm = rsqrt_magic(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))));
+        else norm = rsqrt_norm(__fadd_rn(mean_old, __fmul_rn(dslope, (float)(ind - lo))), exact);
         float2 v = spec[ind];
         v.x = __fmul_rn(v.x, norm);
         v.y = __fmul_rn(v.y, norm);
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_scale_warp(const i
 }
 
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
-                  unsigned numbins, int maxlen, cudaStream_t st) {
+                  unsigned numbins, int maxlen, cudaStream_t st, int exact) {
     if (maxlen <= kWarpBlockMax) {
         const size_t smem = sizeof(uint32_t) * (size_t)kWarpsPerCta * (256 + maxlen);
         if (smem > 48 * 1024 &&
@@ -220,7 +221,7 @@ int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d
             d_bstart, d_blen, spec, d_med, nblocks, maxlen);
         if (cudaGetLastError() != cudaSuccess) return -1;
         k_whiten_scale_warp<<<(nblocks + kWarpsPerCta) / kWarpsPerCta, 32 * kWarpsPerCta, 0, st>>>(
-            d_bstart, d_blen, d_med, nblocks, spec, numbins);
+            d_bstart, d_blen, d_med, nblocks, spec, numbins, exact);
         return cudaGetLastError() == cudaSuccess ? 0 : -1;
     }
     size_t smem = sizeof(uint32_t) * (size_t)maxlen;
@@ -231,7 +232,7 @@ int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d
     }
     k_whiten_medians<<<nblocks, 256, smem, st>>>(d_bstart, d_blen, spec, d_med);
     if (cudaGetLastError() != cudaSuccess) return -1;
-    k_whiten_scale<<<nblocks + 1, 256, 0, st>>>(d_bstart, d_blen, d_med, nblocks, spec, numbins);
+    k_whiten_scale<<<nblocks + 1, 256, 0, st>>>(d_bstart, d_blen, d_med, nblocks, spec, numbins, exact);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

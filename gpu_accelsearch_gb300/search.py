@@ -120,7 +120,7 @@ def autotune(zmax=200, numharm=8, fftlens=(4096, 8192, 16384), steps=64, templat
 class AccelSearch:
     def __init__(self, zmax=200, numharm=8, fftlen=8192, uselen=0, sigma=6.0, numindep=1.0,
                  whiten_initbuf=6, whiten_maxbuf=200, template_fp16=False, chunk_segments=0,
-                 cand_capacity=0, device=0):
+                 cand_capacity=0, device=0, exact_rsqrt=False):
         L = N.lib()
         cfg = N.Config()
         L.accel_config_init(C.byref(cfg))
@@ -129,6 +129,7 @@ class AccelSearch:
         cfg.whiten_initbuf, cfg.whiten_maxbuf = whiten_initbuf, whiten_maxbuf
         cfg.template_fp16 = int(bool(template_fp16))
         cfg.chunk_segments, cfg.cand_capacity, cfg.device = chunk_segments, cand_capacity, device
+        cfg.exact_rsqrt = int(bool(exact_rsqrt))
         self.config = cfg
         self.kwargs = dict(zmax=zmax, numharm=numharm, fftlen=fftlen, template_fp16=template_fp16,
                            chunk_segments=chunk_segments, device=device)

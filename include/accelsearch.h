@@ -49,7 +49,10 @@ typedef struct accel_config {
     int chunk_segments;     /* segments per launch group (0: automatic)          */
     long long cand_capacity;/* raw candidates kept per search (0: automatic)     */
     int device;             /* CUDA device ordinal                               */
-    int reserved[7];
+    int exact_rsqrt;        /* 1: whitening and segment normalisation use an IEEE */
+                            /* 1/sqrt instead of the reference's magic-constant  */
+                            /* approximation (bpd_math.c:94-105; ~1.75e-3 error) */
+    int reserved[6];
 } accel_config;
 
 typedef struct accel_harmonic {

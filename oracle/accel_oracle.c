@@ -40,6 +40,17 @@ float orc_rsqrt_magic(float x)
     return y * (1.5f - h);
 }
 
+/* Normalisation mode: 0 = the magic-constant rsqrt above (the reference's
+ * arithmetic), 1 = IEEE single-precision 1/sqrt(x) (correctly rounded sqrt,
+ * then a correctly rounded divide) -- the GPU build's exact option. */
+static int orc_exact_rsqrt = 0;
+void orc_set_exact_rsqrt(int on) { orc_exact_rsqrt = on != 0; }
+float orc_rsqrt_norm(float x)
+{
+    if (orc_exact_rsqrt) return 1.0f / sqrtf(x);
+    return orc_rsqrt_magic(x);
+}
+
 static int cmp_float(const void *a, const void *b)
 {
     float x = *(const float *)a, y = *(const float *)b;
@@ -283,7 +294,7 @@ void orc_deredden(float *c, unsigned numbins, int initialbuflen, int maxbuflen)
     }
     int buflen = initialbuflen;
     float mean_old = (float)(orc_select_lower_median(pb + binnum, buflen) / log(2.0));
-    norm = orc_rsqrt_magic(mean_old);
+    norm = orc_rsqrt_norm(mean_old);
     for (ind = numwrote; ind < binnum + buflen / 2; ind++) {
         c[2 * ind] *= norm;
         c[2 * ind + 1] *= norm;
@@ -299,7 +310,7 @@ void orc_deredden(float *c, unsigned numbins, int initialbuflen, int maxbuflen)
         for (k = 0, ind = numwrote; ind < binnum + buflen / 2; k++, ind++) {
             float lv = dslope * (float)k;
             lv = mean_old + lv;
-            norm = orc_rsqrt_magic(lv);
+            norm = orc_rsqrt_norm(lv);
             c[2 * ind] *= norm;
             c[2 * ind + 1] *= norm;
         }
@@ -313,7 +324,7 @@ void orc_deredden(float *c, unsigned numbins, int initialbuflen, int maxbuflen)
     for (k = 0, ind = numwrote; ind < (long)numbins; k++, ind++) {
         float lv = dslope * (float)k;
         lv = mean_old + lv;
-        norm = orc_rsqrt_magic(lv);
+        norm = orc_rsqrt_norm(lv);
         c[2 * ind] *= norm;
         c[2 * ind + 1] *= norm;
     }
@@ -396,7 +407,7 @@ int orc_segment_data(const float *wspec, long numbins, int rlo, double rhi, int 
         float b = amp[2 * t + 1] * amp[2 * t + 1];
         pw[t] = a + b;
     }
-    double nc = orc_rsqrt_magic((float)(orc_select_lower_median(pw, numdata) / log(2.0)));
+    double nc = orc_rsqrt_norm((float)(orc_select_lower_median(pw, numdata) / log(2.0)));
     for (int t = 0; t < numdata; t++) {
         amp[2 * t] = (float)(amp[2 * t] * nc);
         amp[2 * t + 1] = (float)(amp[2 * t + 1] * nc);

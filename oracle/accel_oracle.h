@@ -24,6 +24,8 @@ extern "C" {
 
 /* ---- reference host math (bpd_math.c, bpd_fresnl.c) ------------------- */
 float  orc_rsqrt_magic(float x);                       /* bpd_math.c:94-105  */
+void   orc_set_exact_rsqrt(int on);                   /* GPU build's exact-rsqrt option */
+float  orc_rsqrt_norm(float x);                        /* the normalisation in force  */
 float  orc_select_lower_median(const float *a, int n); /* bpd_math.c:20-91   */
 long long orc_next_pow2(long long x);                  /* bpd_math.c:113-122 */
 int    orc_fresnl(double x, double *s, double *c);     /* bpd_fresnl.c:160-200 */

@@ -43,6 +43,8 @@ def lib():
         fp, dp, ip = (C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int))
         sig = {
             "orc_rsqrt_magic": (C.c_float, [C.c_float]),
+            "orc_rsqrt_norm": (C.c_float, [C.c_float]),
+            "orc_set_exact_rsqrt": (None, [C.c_int]),
             "orc_select_lower_median": (C.c_float, [fp, C.c_int]),
             "orc_next_pow2": (C.c_longlong, [C.c_longlong]),
             "orc_fresnl": (C.c_int, [C.c_double, dp, dp]),
@@ -94,6 +96,17 @@ def _ip(a):
 # ---------------------------------------------------------------- scalars
 def rsqrt_magic(x: float) -> float:
     return lib().orc_rsqrt_magic(x)
+
+
+def set_exact_rsqrt(on: bool) -> None:
+    """Switch the oracle's normalisations (deredden, segment norms) between
+    the reference's magic-constant rsqrt (default) and IEEE 1/sqrtf -- the
+    GPU build's exact_rsqrt option."""
+    lib().orc_set_exact_rsqrt(int(bool(on)))
+
+
+def rsqrt_norm(x: float) -> float:
+    return lib().orc_rsqrt_norm(x)
 
 
 def lower_median(a) -> float:
@@ -324,7 +337,7 @@ def step_norms(wspec, zmax, bank_numharm, uselen, rlo, step, numharm):
         ok = (idx >= 0) & (idx < len(wspec))
         v[ok] = wspec[idx[ok]]
         pw = (v.real * v.real + v.imag * v.imag).astype(np.float32)
-        nrm = rsqrt_magic(float(np.float64(lower_median(pw)) / log(2.0)))
+        nrm = rsqrt_norm(float(np.float64(lower_median(pw)) / log(2.0)))
         out.append(float(nrm) * float(nrm))
     return out
 

@@ -105,3 +105,24 @@ def test_step_geometry_and_segments(pins, which):
             assert rhi == st["rhi"][h]
             segs.append(O.segment_data(w, rlo, rhi, int(g[5]), int(g[4])))
         assert sha(np.concatenate(segs).view(np.float32)) == st["data_sha"], st["step"]
+
+
+def test_exact_rsqrt_mode_switch():
+    # the oracle's exact mode is IEEE 1/sqrtf; the default stays the
+    # reference's magic-constant rsqrt, and the switch is reversible
+    xs = np.linspace(0.01, 40.0, 997, dtype=np.float32)
+    magic = np.array([O.rsqrt_magic(float(x)) for x in xs], np.float32)
+    assert np.array_equal(np.array([O.rsqrt_norm(float(x)) for x in xs], np.float32), magic)
+    O.set_exact_rsqrt(True)
+    try:
+        got = np.array([O.rsqrt_norm(float(x)) for x in xs], np.float32)
+        spec = synth_red_spectrum(1 << 14, seed=3)
+        w_exact = O.deredden(spec)
+    finally:
+        O.set_exact_rsqrt(False)
+    assert np.array_equal(got, np.float32(1.0) / np.sqrt(xs))
+    rel = np.abs(magic.astype(np.float64) / got - 1)
+    assert 1e-4 < rel.max() < 2e-3
+    w_magic = O.deredden(spec)
+    assert not np.array_equal(w_exact, w_magic)
+    assert np.abs(np.abs(w_exact) / np.abs(w_magic) - 1)[1:].max() < 2e-3
