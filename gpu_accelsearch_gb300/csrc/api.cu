@@ -150,13 +150,19 @@ struct ProfScope {
         c->stats.kind_launches[kind] += nlaunch;
         if (c->profiling) {
             a = take_event(c);
-            cudaEventRecord(a, st);
+            record(a);
         }
+    }
+    // inside a graph capture the events become event-record nodes, timed
+    // when the graph runs
+    void record(cudaEvent_t e) const {
+        if (c->capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+        else cudaEventRecord(e, st);
     }
     ~ProfScope() {
         if (a) {
             cudaEvent_t b = take_event(c);
-            cudaEventRecord(b, st);
+            record(b);
             c->pending.push_back({kind, a, b});
         }
     }
@@ -555,6 +561,62 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
     return ACCEL_OK;
 }
 
+// Record the launches that issue() makes into a CUDA graph and launch it on
+// the context's stream.  issue() runs against two non-blocking capture
+// streams standing in for stream and stream2, so that nothing else ordered
+// with the legacy default stream can join the capture.  The executable
+// graph is kept: a later capture of the same shape (same launch groups and
+// kernels, other arguments) updates it in place, any other is instantiated
+// anew.
+int launch_as_graph(accel_ctx* c, const std::function<int()>& issue) {
+    if (!c->gcap) CK(cudaStreamCreateWithFlags(&c->gcap, cudaStreamNonBlocking));
+    if (!c->gcap2) CK(cudaStreamCreateWithFlags(&c->gcap2, cudaStreamNonBlocking));
+    cudaStream_t s0 = c->stream, s1 = c->stream2;
+    c->stream = c->gcap;
+    c->stream2 = s1 ? c->gcap2 : nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        c->stream = s0;
+        c->stream2 = s1;
+        return set_err(ACCEL_ERR_CUDA, "cudaStreamBeginCapture failed: %s", cudaGetErrorString(e));
+    }
+    c->capturing = true;
+    const int rc = issue();
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(c->stream, &g);
+    c->capturing = false;
+    c->stream = s0;
+    c->stream2 = s1;
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : set_err(ACCEL_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    }
+    bool built = false;
+    if (c->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(c->gexec, g, &info) != cudaSuccess) {
+            cudaGetLastError();  // not an error: the shape changed, instantiate anew
+            cudaGraphExecDestroy(c->gexec);
+            c->gexec = nullptr;
+        }
+    }
+    if (!c->gexec) {
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        if (e != cudaSuccess) {
+            c->gexec = nullptr;
+            cudaGraphDestroy(g);
+            return set_err(ACCEL_ERR_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+        }
+        built = true;
+    }
+    cudaGraphDestroy(g);
+    CK(cudaGraphLaunch(c->gexec, c->stream));
+    c->stats.graph_launches++;
+    if (built) c->stats.graph_builds++;
+    return ACCEL_OK;
+}
+
 // Segment table: one entry per (trial, step), trial-major.
 struct SegSpan {
     std::vector<int> trial, step;
@@ -586,54 +648,61 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
             d.trial = i;
             d.step = (int)s;
         }
-    CK(cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), c->stream));
-    if (total > 0)
-        CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
-                           c->stream));
-    const bool overlap = c->overlap && !c->fused_sum && c->planes2 && c->stream2;
-    if (overlap) {
-        // fork: stream2 starts after everything queued so far on the main stream
-        CK(cudaEventRecord(c->ev_fork, c->stream));
-        CK(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
-    }
-    int prepared = 0;  // trials [0, prepared) have been prepared
-    auto prepare_upto = [&](int last) -> int {
-        for (; prepare && prepared <= last && prepared < ntrials; prepared++) {
-            const int r = prepare(prepared);
-            if (r) return r;
+    // everything from clearing the candidate count to the last harmonic sum:
+    // launched directly, or recorded into the context's CUDA graph
+    auto issue = [&]() -> int {
+        CK(cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), c->stream));
+        if (total > 0)
+            CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
+                               c->stream));
+        const bool overlap = c->overlap && !c->fused_sum && c->planes2 && c->stream2;
+        if (overlap) {
+            // fork: stream2 starts after everything queued so far on the main stream
+            CK(cudaEventRecord(c->ev_fork, c->stream));
+            CK(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+        }
+        int prepared = 0;  // trials [0, prepared) have been prepared
+        auto prepare_upto = [&](int last) -> int {
+            for (; prepare && prepared <= last && prepared < ntrials; prepared++) {
+                const int r = prepare(prepared);
+                if (r) return r;
+            }
+            return ACCEL_OK;
+        };
+        for (long long g = 0, k = 0; g < total; g += c->chunk, k++) {
+            int n = (int)std::min<long long>(c->chunk, total - g);
+            rc = prepare_upto(c->h_segs[g + n - 1].trial);
+            if (rc) return rc;
+            if (!overlap) {
+                rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true,
+                               c->fused_sum != 0);
+                if (rc) return rc;
+                continue;
+            }
+            // group k: planes into buffer k%2 on the main stream, summed on stream2
+            const int b = (int)(k & 1);
+            float* pb = b ? c->planes2 : c->planes;
+            if (k >= 2) CK(cudaStreamWaitEvent(c->stream, c->ev_sum[b], 0));  // buffer b free again
+            rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, true, true, false);
+            if (rc) return rc;
+            CK(cudaEventRecord(c->ev_plane[b], c->stream));
+            CK(cudaStreamWaitEvent(c->stream2, c->ev_plane[b], 0));
+            rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, false, false, true, false,
+                           c->stream2);
+            if (rc) return rc;
+            CK(cudaEventRecord(c->ev_sum[b], c->stream2));
+        }
+        rc = prepare_upto(ntrials - 1);
+        if (rc) return rc;
+        if (overlap) {
+            // join: the main stream continues after the last sum
+            CK(cudaEventRecord(c->ev_fork, c->stream2));
+            CK(cudaStreamWaitEvent(c->stream, c->ev_fork, 0));
         }
         return ACCEL_OK;
     };
-    for (long long g = 0, k = 0; g < total; g += c->chunk, k++) {
-        int n = (int)std::min<long long>(c->chunk, total - g);
-        rc = prepare_upto(c->h_segs[g + n - 1].trial);
-        if (rc) return rc;
-        if (!overlap) {
-            rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true,
-                           c->fused_sum != 0);
-            if (rc) return rc;
-            continue;
-        }
-        // group k: planes into buffer k%2 on the main stream, summed on stream2
-        const int b = (int)(k & 1);
-        float* pb = b ? c->planes2 : c->planes;
-        if (k >= 2) CK(cudaStreamWaitEvent(c->stream, c->ev_sum[b], 0));  // buffer b free again
-        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, true, true, false);
-        if (rc) return rc;
-        CK(cudaEventRecord(c->ev_plane[b], c->stream));
-        CK(cudaStreamWaitEvent(c->stream2, c->ev_plane[b], 0));
-        rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, pb, false, false, true, false,
-                       c->stream2);
-        if (rc) return rc;
-        CK(cudaEventRecord(c->ev_sum[b], c->stream2));
-    }
-    rc = prepare_upto(ntrials - 1);
+    rc = (c->use_graph && !prepare) ? launch_as_graph(c, issue) : issue();
     if (rc) return rc;
-    if (overlap) {
-        // join: the main stream continues after the last sum
-        CK(cudaEventRecord(c->ev_fork, c->stream2));
-        CK(cudaStreamWaitEvent(c->stream, c->ev_fork, 0));
-    }
     CK(cudaMemcpyAsync(c->h_ncand, c->d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -708,6 +777,9 @@ void free_ctx(accel_ctx* c) {
     cudaFree(c->dbuf);
     cudaFree(c->planes);
     cudaFree(c->planes2);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->gcap) cudaStreamDestroy(c->gcap);
+    if (c->gcap2) cudaStreamDestroy(c->gcap2);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (cudaEvent_t e : c->copy_ev) cudaEventDestroy(e);
@@ -868,6 +940,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->hsum_rowwise = !c->hsum_tiled;
     t->serial_sum = !c->overlap;
     t->hsum_pipelined = c->hsum_pipe;
+    t->graph = c->use_graph;
     return ACCEL_OK;
 }
 
@@ -882,6 +955,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->hsum_tiled = t->hsum_rowwise == 0;
     c->overlap = t->serial_sum == 0;
     c->hsum_pipe = t->hsum_pipelined != 0;
+    c->use_graph = t->graph != 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaStreamSynchronize(c->stream2));

@@ -68,6 +68,12 @@ struct accel_ctx {
     bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
     int hsum_tiled = 1;
     int hsum_pipe = 0;      // persistent pipelined tile kernel
+    // CUDA graph of a device-resident search: recorded on two non-blocking
+    // capture streams standing in for stream/stream2, launched on stream
+    int use_graph = 0;
+    bool capturing = false;   // launches are being recorded, not run
+    cudaStream_t gcap = nullptr, gcap2 = nullptr;
+    cudaGraphExec_t gexec = nullptr;
     int tile_floats = 0;
     float2* dbuf = nullptr;
     float* planes = nullptr;

@@ -58,7 +58,7 @@ class ServerStats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("chunk_segments", C.c_int), ("plane_split", C.c_int), ("fused_sum", C.c_int),
                 ("hsum_rowwise", C.c_int), ("serial_sum", C.c_int), ("hsum_pipelined", C.c_int),
-                ("reserved", C.c_int * 2)]
+                ("graph", C.c_int), ("reserved", C.c_int * 1)]
 
 
 class Optimized(C.Structure):
@@ -70,7 +70,8 @@ class Optimized(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 6),
                 ("kind_ms", C.c_double * 6), ("segments", C.c_longlong),
-                ("cells", C.c_longlong), ("search_ms", C.c_double), ("searches", C.c_longlong)]
+                ("cells", C.c_longlong), ("search_ms", C.c_double), ("searches", C.c_longlong),
+                ("graph_launches", C.c_longlong), ("graph_builds", C.c_longlong)]
 
 
 KINDS = ["prep", "plane", "hsum", "whiten", "rfft", "fund"]

@@ -197,10 +197,10 @@ class AccelSearch:
         return {"chunk_segments": t.chunk_segments, "plane_split": t.plane_split,
                 "fused_sum": t.fused_sum,
                 "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum,
-                "hsum_pipelined": t.hsum_pipelined}
+                "hsum_pipelined": t.hsum_pipelined, "graph": t.graph}
 
     def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
-                   hsum_rowwise=None, serial_sum=None, hsum_pipelined=None):
+                   hsum_rowwise=None, serial_sum=None, hsum_pipelined=None, graph=None):
         cur = self.tuning()
         t = N.Tuning()
         t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
@@ -209,6 +209,7 @@ class AccelSearch:
         t.hsum_rowwise = cur["hsum_rowwise"] if hsum_rowwise is None else int(hsum_rowwise)
         t.serial_sum = cur["serial_sum"] if serial_sum is None else int(serial_sum)
         t.hsum_pipelined = cur["hsum_pipelined"] if hsum_pipelined is None else int(hsum_pipelined)
+        t.graph = cur["graph"] if graph is None else int(graph)
         N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
 
     def profile(self, enable: bool = True):
@@ -219,6 +220,7 @@ class AccelSearch:
         N.check(N.lib().accel_get_stats(self._h, C.byref(st)))
         return {"launches": st.launches, "segments": st.segments, "cells": st.cells,
                 "search_ms": st.search_ms, "searches": st.searches,
+                "graph_launches": st.graph_launches, "graph_builds": st.graph_builds,
                 "kinds": {k: {"launches": st.kind_launches[i], "ms": st.kind_ms[i]}
                           for i, k in enumerate(N.KINDS)}}
 

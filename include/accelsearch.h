@@ -88,6 +88,9 @@ typedef struct accel_stats {
     double search_ms;                   /* CUDA-event time of the accel_search* */
                                         /* calls, first copy to last read-back */
     long long searches;
+    long long graph_launches;           /* searches launched as a CUDA graph   */
+    long long graph_builds;             /* of which the graph was instantiated */
+                                        /* anew (the others updated it)        */
 } accel_stats;
 
 /* Launch shape of a context's search (accel_get_tuning/accel_set_tuning). */
@@ -106,7 +109,13 @@ typedef struct accel_tuning {
     int hsum_pipelined;     /* 1: tiled sum from persistent CTAs that overlap */
                             /* the next tiles' copies with the current sums   */
                             /* (producer warps); 0: one CTA per tile          */
-    int reserved[2];
+    int graph;              /* 1: a search from device-resident data records  */
+                            /* its launch groups into a CUDA graph and        */
+                            /* launches that (the executable graph is kept    */
+                            /* and updated in place while the launch sequence */
+                            /* keeps its shape); searches that copy series    */
+                            /* from host memory launch directly               */
+    int reserved[1];
 } accel_tuning;
 
 typedef struct accel_ctx accel_ctx;
