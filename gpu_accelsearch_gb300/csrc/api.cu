@@ -1106,10 +1106,6 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
             CK(cudaMalloc(&t.spec, sizeof(float2) * (n / 2 + 1)));
             t.n = n;
         }
-        if (!on_device) {
-            CK(cudaMemcpyAsync(t.series, series[i], sizeof(float) * n, cudaMemcpyHostToDevice, c->copy_stream));
-            CK(cudaEventRecord(c->copy_ev[i], c->copy_stream));
-        }
     }
     for (int i = 0; i < ntrials; i++) {
         TrialBuf& t = c->trials[i];
@@ -1118,14 +1114,33 @@ int accel_search(accel_ctx* c, int ntrials, const float* const* series, const lo
         t.numbins = nsamples[i] / 2;
         rlo[i] = accel_first_bin(nsamples[i], dt[i]);
     }
-    // from host memory, a trial's R2C and whitening are issued just before
+    // From host memory, a trial's R2C and whitening are issued just before
     // the first launch group that needs it, so that the copies of later
     // trials overlap the search; series already on the device are all
-    // prepared first
+    // prepared first.  The copies are issued kCopyAhead trials ahead of the
+    // trial being prepared rather than all before the first launch group:
+    // with every copy of a 256-trial batch queued up front, the device time
+    // of host-fed searches on a GB300 grew from call to call (1.53 to 1.60 s
+    // over 16 calls, while copies of the same pinned buffers slowed down);
+    // issued a few trials ahead it stays within 0.3 % of the search from
+    // device-resident series.  The host still runs far ahead of the GPU, so
+    // the copies stay ahead of the search.
+    constexpr int kCopyAhead = 8;
+    int copied = 0;  // copies of trials [0, copied) have been issued
+    auto copy_upto = [&](int last) -> int {
+        for (; copied <= last && copied < ntrials; copied++) {
+            CK(cudaMemcpyAsync(c->trials[copied].series, series[copied], sizeof(float) * nsamples[copied],
+                               cudaMemcpyHostToDevice, c->copy_stream));
+            CK(cudaEventRecord(c->copy_ev[copied], c->copy_stream));
+        }
+        return ACCEL_OK;
+    };
     auto prepare = [&](int i) -> int {
         TrialBuf& t = c->trials[i];
         const float* src = series[i];
         if (!on_device) {
+            const int r = copy_upto(i + kCopyAhead);
+            if (r) return r;
             CK(cudaStreamWaitEvent(c->stream, c->copy_ev[i], 0));
             src = t.series;
         }

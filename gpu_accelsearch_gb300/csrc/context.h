@@ -70,7 +70,7 @@ struct accel_ctx {
     int hsum_pipe = 0;      // persistent pipelined tile kernel
     // CUDA graph of a device-resident search: recorded on two non-blocking
     // capture streams standing in for stream/stream2, launched on stream
-    int use_graph = 0;
+    int use_graph = 1;
     bool capturing = false;   // launches are being recorded, not run
     cudaStream_t gcap = nullptr, gcap2 = nullptr;
     cudaGraphExec_t gexec = nullptr;

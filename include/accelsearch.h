@@ -109,12 +109,13 @@ typedef struct accel_tuning {
     int hsum_pipelined;     /* 1: tiled sum from persistent CTAs that overlap */
                             /* the next tiles' copies with the current sums   */
                             /* (producer warps); 0: one CTA per tile          */
-    int graph;              /* 1: a search from device-resident data records  */
-                            /* its launch groups into a CUDA graph and        */
-                            /* launches that (the executable graph is kept    */
-                            /* and updated in place while the launch sequence */
-                            /* keeps its shape); searches that copy series    */
-                            /* from host memory launch directly               */
+    int graph;              /* 1 (default): a search from device-resident     */
+                            /* data records its launch groups into a CUDA     */
+                            /* graph and launches that (the executable graph  */
+                            /* is kept and updated in place while the launch  */
+                            /* sequence keeps its shape); 0: direct launches. */
+                            /* Searches that copy series from host memory     */
+                            /* always launch directly                         */
     int reserved[1];
 } accel_tuning;
 
