@@ -95,3 +95,35 @@ def test_graph_series_on_device_and_host(trials):
         s.search([t["x"]], 64e-6)
         assert np.array_equal(s.candidates(), want)
         assert s.stats()["graph_launches"] == 1
+
+
+def test_search_on_caller_stream(trials):
+    # accel_set_stream: the search runs on the caller's stream, ordered after
+    # the caller's still-pending kernels that produce its input (a spin of
+    # about 0.1 s delays them), as a graph and as direct launches
+    import ctypes as C
+
+    from gpu_accelsearch_gb300 import native as N
+    from gpu_accelsearch_gb300.search import AccelSearch
+    t = trials[0]
+    src = dev(t["w"])
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048) as s:
+        s.set_power_cuts(CUTS)
+        s.set_tuning(chunk_segments=48, graph=0)
+        want = _search(s, [src], [t], 1)
+        side = torch.cuda.Stream()
+        torch.cuda.synchronize()
+        for graph in (1, 0):
+            s.set_tuning(graph=graph)
+            with torch.cuda.stream(side):
+                d = torch.zeros_like(src)
+                if hasattr(torch.cuda, "_sleep"):
+                    torch.cuda._sleep(200_000_000)
+                d.copy_(src)
+                N.check(N.lib().accel_set_stream(s._h, C.c_void_p(side.cuda_stream)))
+                try:
+                    got = _search(s, [d], [t], 1)
+                finally:
+                    N.check(N.lib().accel_set_stream(s._h, None))
+            torch.cuda.synchronize()
+            assert np.array_equal(got, want), graph
