@@ -382,14 +382,31 @@ int ensure_segs(accel_ctx* c, long long n) {
     return ACCEL_OK;
 }
 
+// Whitening block plan of a spectrum length on the device, cached per
+// length.  The cache keeps the kWhitenPlans most recently used lengths (a
+// request server sees a new length with almost every request); buffers are
+// allocated and freed in stream order on the context's stream, so neither
+// a new length nor an eviction waits for the device.
+constexpr size_t kWhitenPlans = 64;
+
 int whiten_plan(accel_ctx* c, unsigned numbins, WhitenPlanDev** out) {
     auto it = c->wplans.find(numbins);
     if (it != c->wplans.end()) {
+        it->second.last_use = ++c->wplan_clock;
         *out = &it->second;
         return ACCEL_OK;
     }
     if (numbins <= (unsigned)(1 + c->cfg.whiten_initbuf))
         return set_err(ACCEL_ERR_INVALID, "spectrum of %u bins is too short to whiten", numbins);
+    if (c->wplans.size() >= kWhitenPlans) {
+        auto lru = c->wplans.begin();
+        for (auto e = c->wplans.begin(); e != c->wplans.end(); ++e)
+            if (e->second.last_use < lru->second.last_use) lru = e;
+        CK(cudaFreeAsync(lru->second.d_start, c->stream));
+        CK(cudaFreeAsync(lru->second.d_len, c->stream));
+        CK(cudaFreeAsync(lru->second.d_med, c->stream));
+        c->wplans.erase(lru);
+    }
     auto blocks = plan_whiten_blocks(numbins, c->cfg.whiten_initbuf, c->cfg.whiten_maxbuf);
     WhitenPlanDev w;
     w.nb = (int)blocks.size();
@@ -399,11 +416,14 @@ int whiten_plan(accel_ctx* c, unsigned numbins, WhitenPlanDev** out) {
         l[i] = blocks[i].second;
         w.maxlen = std::max(w.maxlen, l[i]);
     }
-    CK(cudaMalloc(&w.d_start, sizeof(int) * w.nb));
-    CK(cudaMalloc(&w.d_len, sizeof(int) * w.nb));
-    CK(cudaMalloc(&w.d_med, sizeof(double) * w.nb));
-    CK(cudaMemcpy(w.d_start, s.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(w.d_len, l.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice));
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&w.d_start), sizeof(int) * w.nb, c->stream));
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&w.d_len), sizeof(int) * w.nb, c->stream));
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&w.d_med), sizeof(double) * w.nb, c->stream));
+    // from pageable memory: staged before the call returns, so the vectors
+    // may go out of scope
+    CK(cudaMemcpyAsync(w.d_start, s.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(w.d_len, l.data(), sizeof(int) * w.nb, cudaMemcpyHostToDevice, c->stream));
+    w.last_use = ++c->wplan_clock;
     auto r = c->wplans.emplace(numbins, w);
     *out = &r.first->second;
     return ACCEL_OK;

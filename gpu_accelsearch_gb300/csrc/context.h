@@ -20,6 +20,7 @@ struct WhitenPlanDev {
     int* d_start = nullptr;
     int* d_len = nullptr;
     double* d_med = nullptr;
+    long long last_use = 0;
 };
 
 struct TrialBuf {
@@ -85,7 +86,8 @@ struct accel_ctx {
     unsigned long long* h_ncand = nullptr;  // pinned
     long long cand_cap = 0;
 
-    std::map<unsigned, WhitenPlanDev> wplans;
+    std::map<unsigned, WhitenPlanDev> wplans;  // by spectrum length, at most kWhitenPlans
+    long long wplan_clock = 0;
     std::map<long long, cufftHandle> fftplans;
     std::map<long long, long long> fftplan_use;  // last use of each plan (LRU)
     long long fftplan_clock = 0;

@@ -5,15 +5,25 @@
 //     (series + spectrum) fits the HBM budget and the active limit, copies
 //     the series in, and runs the R2C transform and whitening on the device;
 //   * builds each launch group from the active requests of one template
-//     bank (one bank per zmax, created on first use), taking their next
-//     overlap-save steps round-robin, so a request admitted while others
-//     are in flight gets steps in the very next group and its work overlaps
-//     with theirs on the device;
+//     bank (one bank per zmax, created on first use), shortest remaining
+//     work first: the bank holding the active request with the least work
+//     left, then that bank's requests in order of remaining steps, as many
+//     steps of each as the group has room for.  A request admitted while
+//     others are in flight joins the very next group that has room, so its
+//     work overlaps with theirs on the device, and a short request overtakes
+//     a long one instead of sharing the GPU with it step by step;
 //   * completes a request when its last step has been summed: candidates
 //     are kept for accel_server_result, its device memory is released and
 //     its latency (submission to completion) recorded.
 // Each segment is computed independently of the others in its group, so a
 // request's result does not depend on what it was batched with.
+//
+// A planner thread makes each request's cuFFT R2C plan when the request is
+// submitted (making a plan for a new length costs about 2 ms of host time,
+// and almost every request of a serving stream has a new length), without
+// work area: the worker runs every transform on one stream with one shared
+// work area.  Plans no queued or active request needs are destroyed once
+// more than kPlanCache of them exist.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -50,8 +60,15 @@ struct Request {
 struct Group {
     accel_ctx* ctx = nullptr;
     std::vector<Request*> active;
-    size_t rr = 0;
 };
+
+struct R2CPlan {
+    cufftHandle plan = 0;
+    size_t work = 0;  // work-area bytes
+    bool ok = false;
+};
+
+constexpr size_t kPlanCache = 256;
 
 }  // namespace
 
@@ -65,8 +82,18 @@ struct accel_server {
     std::deque<Request*> pending;
     std::map<long long, std::unique_ptr<Request>> reqs;
     std::map<int, Group> groups;
-    int group_rr = 0;
     long long next_id = 1;
+    // R2C plans by series length (planner thread; guarded by plan_mu)
+    std::thread planner;
+    std::mutex plan_mu;
+    std::condition_variable plan_cv;
+    bool plan_stop = false;
+    bool plan_evict = false;              // a cached plan lost its last user
+    std::deque<long long> plan_queue;
+    std::map<long long, R2CPlan> plans;
+    std::map<long long, int> plan_users;  // queued or active requests per length
+    void* work = nullptr;                 // shared cuFFT work area (worker thread)
+    size_t work_bytes = 0;
     double bytes_in_use = 0;
     accel_server_stats st{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -77,11 +104,25 @@ namespace {
 
 double request_bytes(long long n) { return 4.0 * n + 8.0 * (n / 2 + 1); }
 
+void release_plan(accel_server* s, long long n) {
+    bool wake = false;
+    {
+        std::lock_guard<std::mutex> lk(s->plan_mu);
+        auto it = s->plan_users.find(n);
+        if (it != s->plan_users.end() && --it->second <= 0) {
+            s->plan_users.erase(it);
+            wake = s->plan_evict = s->plans.size() > kPlanCache;
+        }
+    }
+    if (wake) s->plan_cv.notify_all();
+}
+
 void finish(accel_server* s, Request* r, int rc) {
     if (r->d_series) cudaFreeAsync(r->d_series, s->stream);
     if (r->d_spec) cudaFreeAsync(r->d_spec, s->stream);
     r->d_series = nullptr;
     r->d_spec = nullptr;
+    release_plan(s, r->n);
     r->rc = rc;
     r->t_done = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
@@ -127,8 +168,28 @@ int admit(accel_server* s, Request* r) {
     if (cudaMemcpyAsync(r->d_series, r->host, sizeof(float) * r->n, cudaMemcpyHostToDevice, s->stream) !=
         cudaSuccess)
         return set_error(ACCEL_ERR_CUDA, "request %lld: copy", r->id);
-    rc = do_rfft(c, r->d_series, r->n, r->d_spec);
-    if (!rc) rc = do_whiten(c, r->d_spec, (unsigned)r->numbins);
+    R2CPlan pl;
+    {
+        std::unique_lock<std::mutex> lk(s->plan_mu);
+        s->plan_cv.wait(lk, [&] { return s->plans.count(r->n) != 0; });
+        pl = s->plans[r->n];
+    }
+    if (!pl.ok) return set_error(ACCEL_ERR_CUDA, "request %lld: cuFFT plan for %lld samples", r->id, r->n);
+    if (pl.work > s->work_bytes) {
+        // grow the shared work area (transforms in flight use the old one)
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+            return set_error(ACCEL_ERR_CUDA, "request %lld: stream", r->id);
+        cudaFree(s->work);
+        s->work = nullptr;
+        s->work_bytes = 0;
+        if (cudaMalloc(&s->work, pl.work) != cudaSuccess)
+            return set_error(ACCEL_ERR_NOMEM, "request %lld: cuFFT work area", r->id);
+        s->work_bytes = pl.work;
+    }
+    if (cufftSetWorkArea(pl.plan, s->work) != CUFFT_SUCCESS || cufftSetStream(pl.plan, s->stream) != CUFFT_SUCCESS ||
+        cufftExecR2C(pl.plan, r->d_series, reinterpret_cast<cufftComplex*>(r->d_spec)) != CUFFT_SUCCESS)
+        return set_error(ACCEL_ERR_CUDA, "request %lld: R2C", r->id);
+    rc = do_whiten(c, r->d_spec, (unsigned)r->numbins);
     if (!rc) {
         const long long half = (unsigned short)(c->uselen / 2);
         r->nsteps = 0;
@@ -147,26 +208,24 @@ bool run_one_group(accel_server* s, int zmax) {
     if (ensure_segs(c, cap)) return false;
     const long long half = (unsigned short)(c->uselen / 2);
     s->seg_owner.clear();
-    // round-robin: one step per request per turn until the group is full
-    size_t k = 0, idle = 0;
-    while ((int)s->seg_owner.size() < cap && idle < g.active.size()) {
-        Request* r = g.active[(g.rr + k) % g.active.size()];
-        k++;
-        if (r->next_step >= r->nsteps) {
-            idle++;
-            continue;
+    // shortest remaining work first (ties: earlier submission), every step
+    // of a request before the next one's
+    std::vector<Request*> order(g.active);
+    std::stable_sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
+        return a->nsteps - a->next_step < b->nsteps - b->next_step;
+    });
+    for (Request* r : order) {
+        while ((int)s->seg_owner.size() < cap && r->next_step < r->nsteps) {
+            SegDesc& d = c->h_segs[s->seg_owner.size()];
+            d.spec = r->d_spec;
+            d.numbins = r->numbins;
+            d.startr = r->rlo + r->next_step * half;
+            d.trial = (int)(r->id & 0x7fffffff);
+            d.step = (int)r->next_step;
+            s->seg_owner.push_back({r, r->next_step});
+            r->next_step++;
         }
-        idle = 0;
-        SegDesc& d = c->h_segs[s->seg_owner.size()];
-        d.spec = r->d_spec;
-        d.numbins = r->numbins;
-        d.startr = r->rlo + r->next_step * half;
-        d.trial = (int)(r->id & 0x7fffffff);
-        d.step = (int)r->next_step;
-        s->seg_owner.push_back({r, r->next_step});
-        r->next_step++;
     }
-    g.rr = (g.rr + 1) % std::max<size_t>(1, g.active.size());
     const int n = (int)s->seg_owner.size();
     if (n == 0) return false;
     int rc = ACCEL_OK;
@@ -228,6 +287,51 @@ bool run_one_group(accel_server* s, int zmax) {
     return true;
 }
 
+// Makes the R2C plans of submitted lengths; destroys plans no request
+// needs while more than kPlanCache exist.
+void planner_loop(accel_server* s) {
+    cudaSetDevice(s->cfg.device);
+    for (;;) {
+        long long n = -1;
+        std::vector<cufftHandle> drop;
+        {
+            std::unique_lock<std::mutex> lk(s->plan_mu);
+            s->plan_cv.wait(lk, [&] { return s->plan_stop || !s->plan_queue.empty() || s->plan_evict; });
+            s->plan_evict = false;
+            if (!s->plan_queue.empty()) {
+                n = s->plan_queue.front();
+                s->plan_queue.pop_front();
+            } else if (s->plan_stop) {
+                return;
+            }
+            for (auto it = s->plans.begin(); it != s->plans.end() && s->plans.size() > kPlanCache;) {
+                if (s->plan_users.count(it->first) == 0) {
+                    if (it->second.ok) drop.push_back(it->second.plan);
+                    it = s->plans.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+        }
+        for (cufftHandle h : drop) cufftDestroy(h);
+        if (n < 0) continue;
+        R2CPlan pl;
+        cufftResult e = cufftCreate(&pl.plan);
+        if (e == CUFFT_SUCCESS) e = cufftSetAutoAllocation(pl.plan, 0);
+        if (e == CUFFT_SUCCESS) e = cufftMakePlan1d(pl.plan, (int)n, CUFFT_R2C, 1, &pl.work);
+        pl.ok = e == CUFFT_SUCCESS;
+        if (!pl.ok && pl.plan) {
+            cufftDestroy(pl.plan);
+            pl.plan = 0;
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->plan_mu);
+            s->plans[n] = pl;
+        }
+        s->plan_cv.notify_all();
+    }
+}
+
 void worker_loop(accel_server* s) {
     cudaSetDevice(s->cfg.device);
     for (;;) {
@@ -270,12 +374,24 @@ void worker_loop(accel_server* s) {
             }
             s->groups[r->zmax].active.push_back(r);
         }
-        // next group with work, round-robin over banks
-        std::vector<int> keys;
-        for (auto& kv : s->groups)
-            if (!kv.second.active.empty()) keys.push_back(kv.first);
-        if (keys.empty()) continue;
-        const int zmax = keys[s->group_rr++ % keys.size()];
+        // the bank holding the active request with the least work left
+        // (steps x fundamental cells per step; ties: earlier submission)
+        int zmax = -1;
+        double best = 0.0;
+        long long best_id = 0;
+        for (auto& kv : s->groups) {
+            accel_ctx* c = kv.second.ctx;
+            for (Request* r : kv.second.active) {
+                if (r->next_step >= r->nsteps) continue;
+                const double w = (double)(r->nsteps - r->next_step) * c->uselen * c->numzs0;
+                if (zmax < 0 || w < best || (w == best && r->id < best_id)) {
+                    zmax = kv.first;
+                    best = w;
+                    best_id = r->id;
+                }
+            }
+        }
+        if (zmax < 0) continue;  // (a group completes every request whose steps it issued)
         const auto tg = Clock::now();
         run_one_group(s, zmax);
         s->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
@@ -313,6 +429,7 @@ int accel_server_create(const accel_server_config* cfg, accel_server** out) {
         delete s;
         return set_error(ACCEL_ERR_CUDA, "accel_server_create: %s", cudaGetErrorString(e));
     }
+    s->planner = std::thread(planner_loop, s);
     s->worker = std::thread(worker_loop, s);
     *out = s;
     return ACCEL_OK;
@@ -326,7 +443,17 @@ int accel_server_destroy(accel_server* s) {
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    {
+        std::lock_guard<std::mutex> lk(s->plan_mu);
+        s->plan_stop = true;
+        s->plan_queue.clear();
+    }
+    s->plan_cv.notify_all();
+    if (s->planner.joinable()) s->planner.join();
     cudaStreamSynchronize(s->stream);
+    for (auto& kv : s->plans)
+        if (kv.second.ok) cufftDestroy(kv.second.plan);
+    cudaFree(s->work);
     for (auto& kv : s->groups) accel_destroy(kv.second.ctx);
     for (auto& kv : s->reqs) {
         if (kv.second->d_series) cudaFree(kv.second->d_series);
@@ -340,7 +467,7 @@ int accel_server_destroy(accel_server* s) {
 }
 
 int accel_server_submit(accel_server* s, const float* series, long long n, double dt, int zmax, long long* id) {
-    if (!s || !series || n < 4 || (n & 1) || zmax < 0 || (zmax & 1))
+    if (!s || !series || n < 4 || (n & 1) || n > 0x7fffffffLL || zmax < 0 || (zmax & 1))
         return set_error(ACCEL_ERR_INVALID, "accel_server_submit: bad argument");
     auto r = std::make_unique<Request>();
     r->host = series;
@@ -354,6 +481,14 @@ int accel_server_submit(accel_server* s, const float* series, long long n, doubl
     if (r->bytes > s->cfg.hbm_budget_bytes)
         return set_error(ACCEL_ERR_BUDGET, "request of %.3g bytes exceeds the HBM budget of %.3g", r->bytes,
                          s->cfg.hbm_budget_bytes);
+    {
+        // the planner makes this length's R2C plan while the request waits
+        std::lock_guard<std::mutex> lk(s->plan_mu);
+        if (s->plan_users[n]++ == 0 && s->plans.count(n) == 0 &&
+            std::find(s->plan_queue.begin(), s->plan_queue.end(), n) == s->plan_queue.end())
+            s->plan_queue.push_back(n);
+    }
+    s->plan_cv.notify_all();
     {
         std::lock_guard<std::mutex> lk(s->mu);
         r->id = s->next_id++;
