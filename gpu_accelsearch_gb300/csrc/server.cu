@@ -18,12 +18,13 @@
 // Each segment is computed independently of the others in its group, so a
 // request's result does not depend on what it was batched with.
 //
-// A planner thread makes each request's cuFFT R2C plan when the request is
+// Planner threads make each request's cuFFT R2C plan when the request is
 // submitted (making a plan for a new length costs about 2 ms of host time,
 // and almost every request of a serving stream has a new length), without
 // work area: the worker runs every transform on one stream with one shared
-// work area.  Plans no queued or active request needs are destroyed once
-// more than kPlanCache of them exist.
+// work area.  A queued request is admitted once its plan is ready.  Plans
+// no queued or active request needs are destroyed once more than
+// kPlanCache of them exist.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -32,6 +33,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <vector>
 
@@ -57,9 +59,28 @@ struct Request {
     Clock::time_point t_submit, t_done;
 };
 
+// Device and pinned host buffers of one launch group in flight.
+struct GroupBuf {
+    SegDesc* d_segs = nullptr;
+    SegDesc* h_segs = nullptr;                // pinned
+    RawCand* d_cands = nullptr;
+    unsigned long long* d_ncand = nullptr;    // count, error word
+    unsigned long long* h_ncand = nullptr;    // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr; // the group's kernels
+    cudaEvent_t done = nullptr;               // and its count read-back
+};
+
 struct Group {
     accel_ctx* ctx = nullptr;
     std::vector<Request*> active;
+    GroupBuf buf[2];  // launch groups of this bank alternate between them
+    int next_buf = 0;
+};
+
+// A launched group whose candidates have not been read yet.
+struct Flight {
+    int zmax = -1, b = 0, n = 0, rc = ACCEL_OK;
+    std::vector<std::pair<Request*, long long>> owner;  // per segment: request, step
 };
 
 struct R2CPlan {
@@ -69,6 +90,7 @@ struct R2CPlan {
 };
 
 constexpr size_t kPlanCache = 256;
+constexpr int kPlanners = 4;
 
 }  // namespace
 
@@ -84,7 +106,7 @@ struct accel_server {
     std::map<int, Group> groups;
     long long next_id = 1;
     // R2C plans by series length (planner thread; guarded by plan_mu)
-    std::thread planner;
+    std::vector<std::thread> planners;    // kPlanners threads
     std::mutex plan_mu;
     std::condition_variable plan_cv;
     bool plan_stop = false;
@@ -92,12 +114,13 @@ struct accel_server {
     std::deque<long long> plan_queue;
     std::map<long long, R2CPlan> plans;
     std::map<long long, int> plan_users;  // queued or active requests per length
+    std::set<long long> planning;         // lengths queued or being planned
     void* work = nullptr;                 // shared cuFFT work area (worker thread)
     size_t work_bytes = 0;
     double bytes_in_use = 0;
     accel_server_stats st{};
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::vector<std::pair<Request*, long long>> seg_owner;  // per segment of the current group
+    Flight flight;           // at most one group in flight while the next is built
+    bool in_flight = false;
 };
 
 namespace {
@@ -133,6 +156,22 @@ void finish(accel_server* s, Request* r, int rc) {
     s->cv_done.notify_all();
 }
 
+void free_group(Group& g) {
+    for (GroupBuf& b : g.buf) {
+        cudaFree(b.d_segs);
+        cudaFreeHost(b.h_segs);
+        cudaFree(b.d_cands);
+        cudaFree(b.d_ncand);
+        cudaFreeHost(b.h_ncand);
+        if (b.ev0) cudaEventDestroy(b.ev0);
+        if (b.ev1) cudaEventDestroy(b.ev1);
+        if (b.done) cudaEventDestroy(b.done);
+        b = GroupBuf{};
+    }
+    accel_destroy(g.ctx);
+    g.ctx = nullptr;
+}
+
 accel_ctx* group_ctx(accel_server* s, int zmax, int* rc) {
     Group& g = s->groups[zmax];
     if (g.ctx) return g.ctx;
@@ -154,8 +193,23 @@ accel_ctx* group_ctx(accel_server* s, int zmax, int* rc) {
     accel_get_tuning(g.ctx, &t);
     t.serial_sum = 1;
     accel_set_tuning(g.ctx, &t);
+    for (GroupBuf& b : g.buf) {
+        const int cap = g.ctx->chunk;
+        if (cudaMalloc(&b.d_segs, sizeof(SegDesc) * cap) != cudaSuccess ||
+            cudaMallocHost(&b.h_segs, sizeof(SegDesc) * cap) != cudaSuccess ||
+            cudaMalloc(&b.d_cands, sizeof(RawCand) * g.ctx->cand_cap) != cudaSuccess ||
+            cudaMalloc(&b.d_ncand, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMallocHost(&b.h_ncand, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaEventCreate(&b.ev0) != cudaSuccess || cudaEventCreate(&b.ev1) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming) != cudaSuccess) {
+            *rc = set_error(ACCEL_ERR_NOMEM, "server: launch-group buffers");
+            free_group(g);
+            return nullptr;
+        }
+    }
     return g.ctx;
 }
+
 
 // Copy in, transform and whiten one admitted request (worker thread).
 int admit(accel_server* s, Request* r) {
@@ -198,67 +252,89 @@ int admit(accel_server* s, Request* r) {
     return rc;
 }
 
-// One launch group from the active requests of group zmax.  Returns false
-// when the group had no steps left.
-bool run_one_group(accel_server* s, int zmax) {
+// Build and launch one group from the active requests of bank zmax:
+// shortest remaining work first (ties: earlier submission), every step of
+// a request before the next one's.  The candidate count is copied back
+// asynchronously; complete_group reads the rest.  Returns a flight with
+// n == 0 when the bank had no step left to issue.
+Flight launch_group(accel_server* s, int zmax) {
+    Flight f;
+    f.zmax = zmax;
     Group& g = s->groups[zmax];
     accel_ctx* c = g.ctx;
-    if (!c || g.active.empty()) return false;
+    if (!c || g.active.empty()) return f;
+    f.b = g.next_buf;
+    GroupBuf& B = g.buf[f.b];
     const int cap = c->chunk;
-    if (ensure_segs(c, cap)) return false;
     const long long half = (unsigned short)(c->uselen / 2);
-    s->seg_owner.clear();
-    // shortest remaining work first (ties: earlier submission), every step
-    // of a request before the next one's
     std::vector<Request*> order(g.active);
     std::stable_sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
         return a->nsteps - a->next_step < b->nsteps - b->next_step;
     });
     for (Request* r : order) {
-        while ((int)s->seg_owner.size() < cap && r->next_step < r->nsteps) {
-            SegDesc& d = c->h_segs[s->seg_owner.size()];
+        while ((int)f.owner.size() < cap && r->next_step < r->nsteps) {
+            SegDesc& d = B.h_segs[f.owner.size()];
             d.spec = r->d_spec;
             d.numbins = r->numbins;
             d.startr = r->rlo + r->next_step * half;
             d.trial = (int)(r->id & 0x7fffffff);
             d.step = (int)r->next_step;
-            s->seg_owner.push_back({r, r->next_step});
+            f.owner.push_back({r, r->next_step});
             r->next_step++;
         }
     }
-    const int n = (int)s->seg_owner.size();
-    if (n == 0) return false;
-    int rc = ACCEL_OK;
-    if (cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * n, cudaMemcpyHostToDevice, s->stream) ||
-        cudaMemsetAsync(c->d_ncand, 0, 2 * sizeof(unsigned long long), s->stream))
-        rc = set_error(ACCEL_ERR_CUDA, "server: group upload");
-    cudaEventRecord(s->ev0, s->stream);
-    if (!rc) rc = run_group(c, c->d_segs, n, 0, nullptr, nullptr, nullptr, true, true, true, c->fused_sum != 0);
-    cudaEventRecord(s->ev1, s->stream);
-    std::vector<RawCand> raw;
-    if (!rc) {
-        if (cudaMemcpyAsync(c->h_ncand, c->d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            s->stream) != cudaSuccess ||
-            cudaStreamSynchronize(s->stream) != cudaSuccess)
-            rc = set_error(ACCEL_ERR_CUDA, "server: group");
-        else if (c->h_ncand[1])
-            rc = set_error(ACCEL_ERR_CUDA, "server: a harmonic-sum tile's copy wait timed out");
+    f.n = (int)f.owner.size();
+    if (f.n == 0) return f;
+    g.next_buf ^= 1;
+    if (cudaMemcpyAsync(B.d_segs, B.h_segs, sizeof(SegDesc) * f.n, cudaMemcpyHostToDevice, s->stream) ||
+        cudaMemsetAsync(B.d_ncand, 0, 2 * sizeof(unsigned long long), s->stream))
+        f.rc = set_error(ACCEL_ERR_CUDA, "server: group upload");
+    cudaEventRecord(B.ev0, s->stream);
+    if (!f.rc) {
+        // the harmonic sums append to the context's candidate buffer: this group's
+        RawCand* own_c = c->d_cands;
+        unsigned long long* own_n = c->d_ncand;
+        c->d_cands = B.d_cands;
+        c->d_ncand = B.d_ncand;
+        f.rc = run_group(c, B.d_segs, f.n, 0, nullptr, nullptr, nullptr, true, true, true, c->fused_sum != 0);
+        c->d_cands = own_c;
+        c->d_ncand = own_n;
     }
+    cudaEventRecord(B.ev1, s->stream);
+    if (!f.rc && cudaMemcpyAsync(B.h_ncand, B.d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 s->stream) != cudaSuccess)
+        f.rc = set_error(ACCEL_ERR_CUDA, "server: group count");
+    cudaEventRecord(B.done, s->stream);
+    return f;
+}
+
+// Wait for a launched group, read its candidates, hand them to their
+// requests and complete the requests whose last step it held.
+void complete_group(accel_server* s, Flight& f) {
+    Group& g = s->groups[f.zmax];
+    accel_ctx* c = g.ctx;
+    GroupBuf& B = g.buf[f.b];
+    const long long half = (unsigned short)(c->uselen / 2);
+    int rc = f.rc;
+    std::vector<RawCand> raw;
+    if (!rc && cudaEventSynchronize(B.done) != cudaSuccess) rc = set_error(ACCEL_ERR_CUDA, "server: group");
+    if (!rc && B.h_ncand[1]) rc = set_error(ACCEL_ERR_CUDA, "server: a harmonic-sum tile's copy wait timed out");
     if (!rc) {
-        const long long nr = (long long)std::min<unsigned long long>(*c->h_ncand, (unsigned long long)c->cand_cap);
+        const long long nr = (long long)std::min<unsigned long long>(B.h_ncand[0], (unsigned long long)c->cand_cap);
         raw.resize(nr);
-        if (nr > 0 && cudaMemcpy(raw.data(), c->d_cands, sizeof(RawCand) * nr, cudaMemcpyDeviceToHost) != cudaSuccess)
+        if (nr > 0 && cudaMemcpy(raw.data(), B.d_cands, sizeof(RawCand) * nr, cudaMemcpyDeviceToHost) != cudaSuccess)
             rc = set_error(ACCEL_ERR_CUDA, "server: candidates");
-        if (*c->h_ncand > (unsigned long long)c->cand_cap) rc = set_error(ACCEL_ERR_CAPACITY, "server: candidates");
+        if (B.h_ncand[0] > (unsigned long long)c->cand_cap) rc = set_error(ACCEL_ERR_CAPACITY, "server: candidates");
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->st.gpu_ms += ms;
-        s->st.cells += (long long)n * c->uselen * c->numzs0;
+        if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) s->st.gpu_ms += ms;
+        s->st.cells += (long long)f.n * c->uselen * c->numzs0;
     }
     for (const RawCand& x : raw) {
-        Request* r = s->seg_owner[x.seg].first;
+        Request* r = f.owner[x.seg].first;
+        if (r->state != 1) continue;
         accel_candidate o;
         o.trial = (int)(r->id & 0x7fffffff);
-        o.step = (int)s->seg_owner[x.seg].second;
+        o.step = (int)f.owner[x.seg].second;
         o.r = (double)(r->rlo + o.step * half) + 0.5 * x.ridx;
         o.z = (double)(c->zlo0 + kDz * x.zidx);
         o.numharm = x.numharm;
@@ -266,12 +342,14 @@ bool run_one_group(accel_server* s, int zmax) {
         o.sigma = (float)sigma_of_power_host(x.power, x.numharm, c->cfg.numindep);
         r->cands.push_back(o);
     }
-    for (auto& so : s->seg_owner) so.first->done_steps++;
-    std::vector<Request*> keep;
-    for (Request* r : g.active) {
-        if (rc != ACCEL_OK && r->next_step > 0 && r->state == 1) {
+    for (auto& so : f.owner) {
+        Request* r = so.first;
+        if (r->state != 1) continue;
+        if (rc != ACCEL_OK) {
             finish(s, r, rc);
-        } else if (r->done_steps >= r->nsteps) {
+            continue;
+        }
+        if (++r->done_steps == r->nsteps) {
             std::sort(r->cands.begin(), r->cands.end(), [](const accel_candidate& a, const accel_candidate& b) {
                 if (a.step != b.step) return a.step < b.step;
                 if (a.numharm != b.numharm) return a.numharm < b.numharm;
@@ -279,12 +357,12 @@ bool run_one_group(accel_server* s, int zmax) {
                 return a.r < b.r;
             });
             finish(s, r, ACCEL_OK);
-        } else {
-            keep.push_back(r);
         }
     }
+    std::vector<Request*> keep;
+    for (Request* r : g.active)
+        if (r->state == 1) keep.push_back(r);
     g.active.swap(keep);
-    return true;
 }
 
 // Makes the R2C plans of submitted lengths; destroys plans no request
@@ -327,8 +405,11 @@ void planner_loop(accel_server* s) {
         {
             std::lock_guard<std::mutex> lk(s->plan_mu);
             s->plans[n] = pl;
+            s->planning.erase(n);
         }
         s->plan_cv.notify_all();
+        { std::lock_guard<std::mutex> lk(s->mu); }  // the worker waits on cv_work under mu
+        s->cv_work.notify_all();
     }
 }
 
@@ -338,20 +419,38 @@ void worker_loop(accel_server* s) {
         std::vector<Request*> admitted;
         {
             std::unique_lock<std::mutex> lk(s->mu);
+            // queued requests are admitted in arrival order as their R2C
+            // plans become ready (a request whose plan is still being made
+            // does not hold back the ones behind it); admission stops at
+            // the first request the HBM budget or the active limit cannot
+            // take (lock order: mu, then plan_mu)
+            auto plan_ready = [&](const Request* r) {
+                std::lock_guard<std::mutex> pk(s->plan_mu);
+                return s->plans.count(r->n) != 0;
+            };
+            auto any_ready = [&] {
+                for (const Request* r : s->pending)
+                    if (plan_ready(r)) return true;
+                return false;
+            };
             s->cv_work.wait(lk, [&] {
-                if (s->stop || !s->pending.empty()) return true;
+                if (s->stop || s->in_flight || any_ready()) return true;
                 for (auto& kv : s->groups)
                     if (!kv.second.active.empty()) return true;
                 return false;
             });
             bool any_active = false;
             for (auto& kv : s->groups) any_active |= !kv.second.active.empty();
-            if (s->stop && s->pending.empty() && !any_active) return;
-            while (!s->pending.empty()) {
-                Request* r = s->pending.front();
+            if (s->stop && s->pending.empty() && !any_active && !s->in_flight) return;
+            for (auto it = s->pending.begin(); it != s->pending.end();) {
+                Request* r = *it;
                 if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) break;
                 if (s->bytes_in_use + r->bytes > s->cfg.hbm_budget_bytes) break;
-                s->pending.pop_front();
+                if (!plan_ready(r)) {
+                    ++it;
+                    continue;
+                }
+                it = s->pending.erase(it);
                 s->bytes_in_use += r->bytes;
                 s->st.admitted++;
                 s->st.active++;
@@ -391,9 +490,20 @@ void worker_loop(accel_server* s) {
                 }
             }
         }
-        if (zmax < 0) continue;  // (a group completes every request whose steps it issued)
+        // launch the next group, then read back the one before it: the
+        // host's candidate handling and the next group's set-up overlap the
+        // GPU's work
         const auto tg = Clock::now();
-        run_one_group(s, zmax);
+        Flight next;
+        if (zmax >= 0) next = launch_group(s, zmax);
+        if (s->in_flight) {
+            complete_group(s, s->flight);
+            s->in_flight = false;
+        }
+        if (next.n > 0) {
+            s->flight = std::move(next);
+            s->in_flight = true;
+        }
         s->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
     }
 }
@@ -423,13 +533,11 @@ int accel_server_create(const accel_server_config* cfg, accel_server** out) {
     if (s->cfg.chunk_segments <= 0) s->cfg.chunk_segments = 128;
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
-    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e != cudaSuccess) {
         delete s;
         return set_error(ACCEL_ERR_CUDA, "accel_server_create: %s", cudaGetErrorString(e));
     }
-    s->planner = std::thread(planner_loop, s);
+    for (int i = 0; i < kPlanners; i++) s->planners.emplace_back(planner_loop, s);
     s->worker = std::thread(worker_loop, s);
     *out = s;
     return ACCEL_OK;
@@ -449,18 +557,17 @@ int accel_server_destroy(accel_server* s) {
         s->plan_queue.clear();
     }
     s->plan_cv.notify_all();
-    if (s->planner.joinable()) s->planner.join();
+    for (std::thread& t : s->planners)
+        if (t.joinable()) t.join();
     cudaStreamSynchronize(s->stream);
     for (auto& kv : s->plans)
         if (kv.second.ok) cufftDestroy(kv.second.plan);
     cudaFree(s->work);
-    for (auto& kv : s->groups) accel_destroy(kv.second.ctx);
+    for (auto& kv : s->groups) free_group(kv.second);
     for (auto& kv : s->reqs) {
         if (kv.second->d_series) cudaFree(kv.second->d_series);
         if (kv.second->d_spec) cudaFree(kv.second->d_spec);
     }
-    cudaEventDestroy(s->ev0);
-    cudaEventDestroy(s->ev1);
     cudaStreamDestroy(s->stream);
     delete s;
     return ACCEL_OK;
@@ -484,9 +591,8 @@ int accel_server_submit(accel_server* s, const float* series, long long n, doubl
     {
         // the planner makes this length's R2C plan while the request waits
         std::lock_guard<std::mutex> lk(s->plan_mu);
-        if (s->plan_users[n]++ == 0 && s->plans.count(n) == 0 &&
-            std::find(s->plan_queue.begin(), s->plan_queue.end(), n) == s->plan_queue.end())
-            s->plan_queue.push_back(n);
+        s->plan_users[n]++;
+        if (s->plans.count(n) == 0 && s->planning.insert(n).second) s->plan_queue.push_back(n);
     }
     s->plan_cv.notify_all();
     {
