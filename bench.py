@@ -551,6 +551,9 @@ def run_ours(args):
                    "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
     cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
     serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
+    # the same stream at half the rate: latency when the GPU is not saturated
+    serving_half = (run_serving(args.serving_seconds, local, rate=100.0)
+                    if args.serving_seconds > 0 else None)
     precision = precision_report(args.precision_seeds, local) if args.precision_seeds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
@@ -573,7 +576,7 @@ def run_ours(args):
         "plain": plain,
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "candidates_per_step": ncand,
-        "serving": serving,
+        "serving": serving, "serving_half_load": serving_half,
         "precision_fp16": precision,
     }
     print(json.dumps(line), flush=True)
