@@ -86,6 +86,29 @@ def test_whitening_bit_exact(numbins, init, maxb):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
+def test_whitening_plan_cache_evicts_and_rebuilds():
+    # more spectrum lengths than the context caches whitening plans for
+    # (64): the least recently used plans are freed in stream order and
+    # rebuilt when their length comes back; every result stays bit-exact.
+    # (Where the last slope drives the extrapolated level of the tail below
+    # zero, the reference's inverse square root gives NaN, on the GPU as on
+    # the host; NaN payloads differ between the two, so NaNs compare equal.)
+    from gpu_accelsearch_gb300.search import AccelSearch
+    lengths = [3000 + 37 * i for i in range(70)] + [3000, 3037, 3074]
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048) as s:
+        for numbins in lengths:
+            spec = synth_red_spectrum(numbins + 1, seed=numbins)
+            d = dev(spec)
+            s.whiten(d.data_ptr(), numbins)
+            s.synchronize()
+            want = spec.copy()
+            want[:numbins] = O.deredden(spec[:numbins])
+            got = host_c64(d).view(np.float32)
+            w = want.view(np.float32)
+            same = (got.view(np.uint32) == w.view(np.uint32)) | (np.isnan(got) & np.isnan(w))
+            assert same.all(), numbins
+
+
 def test_segment_spectra(S, trial):
     w = trial["w"]
     startr = [16, 16 + 957, 16 + 957 * 70, 16 + 957 * 135]

@@ -77,3 +77,26 @@ def test_continuous_batching_short_request_overtakes():
         _, lat_short = srv.result(sid)
     assert long_running and short_done_first
     assert lat_short < lat_long
+
+
+def test_many_lengths_and_banks_equal_context_path():
+    # every request a new series length (a new cuFFT plan from the planner
+    # threads, the shared work area growing), two banks, submitted at once
+    from gpu_accelsearch_gb300.search import AccelSearch
+    from gpu_accelsearch_gb300.serving import Server
+    rng = np.random.default_rng(77)
+    reqs = []
+    for i in range(12):
+        n = 2 * int(rng.integers(1 << 14, 1 << 16))
+        z = 50 if i % 3 else 100
+        reqs.append((synth_series(n, seed=300 + i, signals=[(0.1, 0.2 * n + 0.25, 8.0)]), z))
+    with Server(hbm_budget_bytes=4e9, fftlen=2048, numharm=4, chunk_segments=16) as srv:
+        ids = [srv.submit(x, DT, z) for x, z in reqs]
+        for i in ids:
+            assert srv.wait(i, 120)
+        got = [srv.result(i)[0] for i in ids]
+        assert srv.stats()["completed"] == len(reqs)
+    for (x, z), g in zip(reqs, got):
+        with AccelSearch(zmax=z, numharm=4, fftlen=2048) as s:
+            s.search([x], DT)
+            assert same(g, s.candidates()), (x.size, z)
