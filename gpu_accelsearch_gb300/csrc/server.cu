@@ -326,7 +326,9 @@ void complete_group(accel_server* s, Flight& f) {
             rc = set_error(ACCEL_ERR_CUDA, "server: candidates");
         if (B.h_ncand[0] > (unsigned long long)c->cand_cap) rc = set_error(ACCEL_ERR_CAPACITY, "server: candidates");
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) s->st.gpu_ms += ms;
+        cudaEventElapsedTime(&ms, B.ev0, B.ev1);
+        std::lock_guard<std::mutex> lk(s->mu);  // accel_server_get_stats reads under mu
+        s->st.gpu_ms += ms;
         s->st.cells += (long long)f.n * c->uselen * c->numzs0;
     }
     for (const RawCand& x : raw) {
@@ -462,7 +464,11 @@ void worker_loop(accel_server* s) {
         for (Request* r : admitted) {
             const auto ta = Clock::now();
             int rc = admit(s, r);
-            s->st.admit_ms += std::chrono::duration<double, std::milli>(Clock::now() - ta).count();
+            {
+                const double ms = std::chrono::duration<double, std::milli>(Clock::now() - ta).count();
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->st.admit_ms += ms;
+            }
             if (rc) {
                 finish(s, r, rc);
                 continue;
@@ -504,7 +510,11 @@ void worker_loop(accel_server* s) {
             s->flight = std::move(next);
             s->in_flight = true;
         }
-        s->st.group_ms += std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
+        {
+            const double ms = std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->st.group_ms += ms;
+        }
     }
 }
 
