@@ -213,6 +213,40 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
                         "continuous batching (accel_server)"}
 
 
+# ------------------------------------------------------------- dedispersion
+def run_dedisperse(device: int, reps: int = 3):
+    """Incoherent dedispersion upstream of the search: a 1024-channel
+    filterbank (1500 MHz top, 300 MHz band, 64 us samples, N(0,1) float32)
+    into 256 DM trials 0..255 pc cm^-3 of 2^20 samples each, timed with
+    CUDA events after a warm-up (inputs larger than L2)."""
+    import torch
+    from gpu_accelsearch_gb300.dedisperse import dedisperse, dm_delays
+    nchan, nout, ndm = 1024, 1 << 20, 256
+    dl, mx = dm_delays(nchan, 1500.0, -300.0 / nchan, DT, np.arange(ndm, dtype=np.float32))
+    nsamp = nout + mx
+    g = torch.Generator(device="cuda")
+    g.manual_seed(31)
+    fb = torch.randn((nchan, nsamp), generator=g, device="cuda", dtype=torch.float32)
+    out = torch.empty((ndm, nout), device="cuda", dtype=torch.float32)
+    st = torch.cuda.current_stream().cuda_stream
+    dedisperse(fb.data_ptr(), nchan, nsamp, dl, out.data_ptr(), nout, st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        dedisperse(fb.data_ptr(), nchan, nsamp, dl, out.data_ptr(), nout, st)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / reps
+    adds = float(ndm) * nchan * nout
+    byts = 4.0 * (nchan * nsamp + ndm * nout)
+    del fb, out
+    return {"workload": "1024 channels x (2^20 + %d) samples -> 256 DM trials x 2^20 samples" % mx,
+            "ms": sec * 1e3, "dm_samples_per_s": ndm * nout / sec, "adds_per_s": adds / sec,
+            "algorithmic_GBs": byts / sec / 1e9,
+            "note": "algorithmic bytes: the filterbank read once and the trials written once"}
+
+
 # --------------------------------------------------------------- precision
 def precision_report(seeds: int, device: int):
     """FP16 folded templates (scaled per template) against FP32 templates
@@ -550,6 +584,7 @@ def run_ours(args):
     kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
     cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    dedisp = run_dedisperse(local) if args.serving_seconds > 0 else None
     serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
     # the same stream at half the rate: latency when the GPU is not saturated
     serving_half = (run_serving(args.serving_seconds, local, rate=100.0)
@@ -576,7 +611,7 @@ def run_ours(args):
         "plain": plain,
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "candidates_per_step": ncand,
-        "serving": serving, "serving_half_load": serving_half,
+        "serving": serving, "serving_half_load": serving_half, "dedisperse": dedisp,
         "precision_fp16": precision,
     }
     print(json.dumps(line), flush=True)

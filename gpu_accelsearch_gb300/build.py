@@ -5,7 +5,9 @@
 Each CUDA translation unit is compiled in parallel into _build/, then linked
 with cuFFT into gpu_accelsearch_gb300/libaccelsearch.so.  bank.cu is built
 with -fmad=false so that its double-precision template arithmetic rounds
-operation by operation like the reference's host code.
+operation by operation like the reference's host code; compat.cu and
+dedisperse.cu keep the host compiler from contracting multiply-adds, so
+that their host arithmetic gives the same numbers on every host.
 """
 from __future__ import annotations
 
@@ -23,8 +25,9 @@ LIB = os.path.join(PKG, "libaccelsearch.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "bank.cu", "search.cu", "search_plane_lo.cu", "search_plane_hi.cu",
            "search_fund_lo.cu", "search_fund_hi.cu", "tune.cu", "whiten.cu", "compat.cu",
-           "server.cu", "sift.cu", "optimize.cu"]
-EXTRA = {"bank.cu": ["-fmad=false"], "compat.cu": ["-Xcompiler", "-ffp-contract=off"]}
+           "server.cu", "sift.cu", "optimize.cu", "dedisperse.cu"]
+EXTRA = {"bank.cu": ["-fmad=false"], "compat.cu": ["-Xcompiler", "-ffp-contract=off"],
+         "dedisperse.cu": ["-Xcompiler", "-ffp-contract=off"]}
 HEADERS = ["accel_common.cuh", "accel_internal.h", "context.h", "fft_smem.cuh", "search_kernels.cuh"]
 
 

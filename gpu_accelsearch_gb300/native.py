@@ -135,6 +135,10 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)]),
     "accel_server_release": (C.c_int, [_vp, _ll]),
     "accel_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+    "accel_dedisperse_delays": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double,
+                                          C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
+    "accel_dedisperse": (C.c_int, [_vp, C.c_int, _ll, C.POINTER(C.c_int), C.c_int, _vp, _ll, _vp]),
 }
 
 _lib = None

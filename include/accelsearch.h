@@ -324,6 +324,27 @@ int  accel_server_result(accel_server *srv, long long id, accel_candidate *out, 
 int  accel_server_release(accel_server *srv, long long id);
 int  accel_server_get_stats(accel_server *srv, accel_server_stats *out);
 
+/* ------------------------------------------------------- dedispersion */
+/* Incoherent dedispersion, the step upstream of the search that produces
+ * its DM-trial time series (the reference starts from dedispersed series:
+ * README.md names dedispersion as the step before it; no function of the
+ * reference is replaced).  Direct method:
+ *   out[d][t] = sum over channels c, in order, of in[c][t + delay[d][c]].
+ * accel_dedisperse_delays (host only): delay[d][c] = floor(4.148808e3 *
+ * dms[d] * (f_c^-2 - f_ref^-2) / tsamp + 1/2) samples, f_c = f_top_mhz +
+ * c * chan_bw_mhz (chan_bw_mhz < 0 for channels in descending frequency),
+ * f_ref the highest channel frequency; delays is int[ndm][nchan], the
+ * largest delay in *max_delay. */
+int  accel_dedisperse_delays(int nchan, double f_top_mhz, double chan_bw_mhz, double tsamp,
+                             const float *dms, int ndm, int *delays, int *max_delay);
+/* filterbank_dev: float[nchan][nsamp] (time contiguous) on the device;
+ * delays: int[ndm][nchan] in host memory; out_dev: float[ndm][nout] on the
+ * device, nout <= nsamp - max delay.  Runs on cuda_stream (NULL: the legacy
+ * default stream); each DM trial row of out_dev is a series accel_search
+ * takes with series_on_device = 1. */
+int  accel_dedisperse(const float *filterbank_dev, int nchan, long long nsamp, const int *delays,
+                      int ndm, float *out_dev, long long nout, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -363,3 +363,41 @@ def optimize(wspec, r, z, numharm, norms, refine=True):
     hp = [norms[k - 1] * harmonic_power(wspec, r * k / numharm, z * k / numharm)
           for k in range(1, numharm + 1)]
     return r, z, sum(hp), hp
+
+
+# ------------------------------------------------------------ dedispersion
+# Not part of the reference (it starts from dedispersed series).  The
+# restatement follows the standard cold-plasma dispersion delay
+# (Lorimer & Kramer, Handbook of Pulsar Astronomy, eq. 5.1: 4.148808e3 s
+# MHz^2 pc^-1 cm^3 x DM x (f^-2 - f_ref^-2)) and the direct method of
+# incoherent dedispersion; parity for this stage is against this
+# restatement only (no reference implementation exists to pin it).
+DISP_CONST = 4.148808e3
+
+
+def dm_delays(nchan, f_top_mhz, chan_bw_mhz, tsamp, dms):
+    """int32[ndm][nchan] delays in samples, rounded half up, relative to the
+    highest channel frequency (the evaluation order of the library's host
+    code, operation by operation in double precision)."""
+    f = f_top_mhz + np.arange(nchan, dtype=np.float64) * chan_bw_mhz
+    f_ref = max(f_top_mhz, float(f[-1]))
+    inv_ref2 = 1.0 / (f_ref * f_ref)
+    dm = np.asarray(dms, dtype=np.float32).astype(np.float64)[:, None]
+    v = np.floor(DISP_CONST * dm * (1.0 / (f * f) - inv_ref2) / tsamp + 0.5)
+    return v.astype(np.int32)
+
+
+def dedisperse(fb, delays, nout):
+    """float32[ndm][nout]: for each DM trial the channels of fb (float32
+    [nchan][nsamp]) shifted by their delays and added in channel order with
+    float32 rounding after every addition."""
+    fb = np.asarray(fb, dtype=np.float32)
+    ndm, nchan = delays.shape
+    out = np.zeros((ndm, nout), np.float32)
+    for d in range(ndm):
+        acc = np.zeros(nout, np.float32)
+        for c in range(nchan):
+            s = int(delays[d, c])
+            acc += fb[c, s:s + nout]
+        out[d] = acc
+    return out
