@@ -29,14 +29,15 @@ namespace accel {
 
 constexpr int kDdThreads = 256;
 constexpr int kDdPer = 4;  // output samples per thread
-constexpr int kDdD = 8;    // DM trials per CTA
+constexpr int kDdD = 8;    // DM trials per CTA (two int4 of delays per channel)
 constexpr double kDispConst = 4.148808e3;
 
 __global__ void __launch_bounds__(kDdThreads) k_dedisperse(const float* __restrict__ in, int nchan, long long nsamp,
-                                                           const int* __restrict__ delays, int ndm, int ndtile,
+                                                           const int4* __restrict__ dtab, int ndm, int ndtile,
                                                            float* __restrict__ out, long long nout) {
     const long long bid = blockIdx.x;
-    const int d0 = (int)(bid % ndtile) * kDdD;
+    const int tile = (int)(bid % ndtile);
+    const int d0 = tile * kDdD;
     const long long t0 = (bid / ndtile) * (long long)(kDdThreads * kDdPer) + threadIdx.x;
     const int nd = min(kDdD, ndm - d0);
     float acc[kDdD][kDdPer];
@@ -44,17 +45,22 @@ __global__ void __launch_bounds__(kDdThreads) k_dedisperse(const float* __restri
     for (int j = 0; j < kDdD; j++)
 #pragma unroll
         for (int k = 0; k < kDdPer; k++) acc[j][k] = 0.f;
-#pragma unroll 1
+    // dtab row c: the delays of channel c for DM trials [8 tile, 8 tile + 8)
+    // as two int4 (padding trials have delay 0 and are not summed)
+    const int4* __restrict__ dt = dtab + 2LL * tile;
+    const long long dstride = 2LL * ndtile;
+#pragma unroll 4
     for (int c = 0; c < nchan; c++) {
         const float* __restrict__ row = in + (long long)c * nsamp;
+        const int4 lo = __ldg(dt + c * dstride), hi = __ldg(dt + c * dstride + 1);
+        const int dl[kDdD] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
 #pragma unroll
         for (int j = 0; j < kDdD; j++) {
             if (j < nd) {  // uniform over the CTA
-                const int dl = __ldg(delays + (long long)(d0 + j) * nchan + c);
 #pragma unroll
                 for (int k = 0; k < kDdPer; k++) {
                     const long long t = t0 + (long long)k * kDdThreads;
-                    if (t < nout) acc[j][k] = __fadd_rn(acc[j][k], __ldg(row + t + dl));
+                    if (t < nout) acc[j][k] = __fadd_rn(acc[j][k], __ldg(row + t + dl[j]));
                 }
             }
         }
@@ -117,14 +123,20 @@ int accel_dedisperse(const float* filterbank_dev, int nchan, long long nsamp, co
     const long long ntt = (nout + kDdThreads * kDdPer - 1) / (kDdThreads * kDdPer);
     if ((long long)ndtile * ntt > 0x7fffffffLL) return set_error(ACCEL_ERR_UNSUPPORTED, "accel_dedisperse: grid too large");
     cudaStream_t st = (cudaStream_t)cuda_stream;
+    // the kernel's table: channel-major, each channel's delays of all DM
+    // trials padded to whole tiles of kDdD (one 32-byte sector per tile)
+    const long long pad = (long long)ndtile * kDdD;
+    std::vector<int> tab((size_t)(pad * nchan), 0);
+    for (int d = 0; d < ndm; d++)
+        for (int c = 0; c < nchan; c++) tab[(size_t)c * pad + d] = delays[(long long)d * nchan + c];
     int* d_delays = nullptr;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d_delays), sizeof(int) * nd, st);
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d_delays), sizeof(int) * tab.size(), st);
     if (e != cudaSuccess) return set_error(ACCEL_ERR_NOMEM, "accel_dedisperse: %s", cudaGetErrorString(e));
     // from pageable memory: staged before the call returns
-    e = cudaMemcpyAsync(d_delays, delays, sizeof(int) * nd, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(d_delays, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        k_dedisperse<<<(unsigned)(ndtile * ntt), kDdThreads, 0, st>>>(filterbank_dev, nchan, nsamp, d_delays, ndm,
-                                                                      ndtile, out_dev, nout);
+        k_dedisperse<<<(unsigned)(ndtile * ntt), kDdThreads, 0, st>>>(
+            filterbank_dev, nchan, nsamp, reinterpret_cast<const int4*>(d_delays), ndm, ndtile, out_dev, nout);
         e = cudaGetLastError();
     }
     const cudaError_t ef = cudaFreeAsync(d_delays, st);

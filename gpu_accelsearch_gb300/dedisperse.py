@@ -32,3 +32,45 @@ def dedisperse(filterbank_dev: int, nchan: int, nsamp: int, delays: np.ndarray, 
     N.check(N.lib().accel_dedisperse(filterbank_dev, nchan, nsamp,
                                      dl.ctypes.data_as(C.POINTER(C.c_int)), dl.shape[0], out_dev,
                                      nout, stream or None))
+
+
+def _main(argv=None) -> None:
+    """Time one dedispersion of a seeded N(0,1) filterbank on cuda:0:
+    python -m gpu_accelsearch_gb300.dedisperse --nchan 256 --nout 262144 --ndm 64"""
+    import argparse
+    import json
+
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nchan", type=int, default=1024)
+    ap.add_argument("--nout", type=int, default=1 << 20)
+    ap.add_argument("--ndm", type=int, default=256)
+    ap.add_argument("--dm-step", type=float, default=1.0)
+    ap.add_argument("--f-top", type=float, default=1500.0)
+    ap.add_argument("--bandwidth", type=float, default=300.0)
+    ap.add_argument("--tsamp", type=float, default=64e-6)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    dl, mx = dm_delays(a.nchan, a.f_top, -a.bandwidth / a.nchan, a.tsamp,
+                       np.arange(a.ndm, dtype=np.float32) * a.dm_step)
+    nsamp = a.nout + mx
+    g = torch.Generator(device="cuda")
+    g.manual_seed(31)
+    fb = torch.randn((a.nchan, nsamp), generator=g, device="cuda", dtype=torch.float32)
+    out = torch.empty((a.ndm, a.nout), device="cuda", dtype=torch.float32)
+    st = torch.cuda.current_stream().cuda_stream
+    dedisperse(fb.data_ptr(), a.nchan, nsamp, dl, out.data_ptr(), a.nout, st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(a.reps):
+        dedisperse(fb.data_ptr(), a.nchan, nsamp, dl, out.data_ptr(), a.nout, st)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(a.reps, 1)
+    print(json.dumps({"nchan": a.nchan, "nsamp": nsamp, "ndm": a.ndm, "nout": a.nout, "ms": ms,
+                      "adds_per_s": a.ndm * a.nchan * a.nout / (ms / 1e3)}))
+
+
+if __name__ == "__main__":
+    _main()
