@@ -29,7 +29,8 @@ namespace accel {
 
 constexpr int kDdThreads = 256;
 constexpr int kDdPer = 4;  // output samples per thread
-constexpr int kDdD = 8;    // DM trials per CTA (two int4 of delays per channel)
+constexpr int kDdD = 8;    // DM trials per CTA (a multiple of 4: int4 delay loads)
+static_assert(kDdD % 4 == 0, "delays are loaded as int4");
 constexpr double kDispConst = 4.148808e3;
 
 __global__ void __launch_bounds__(kDdThreads) k_dedisperse(const float* __restrict__ in, int nchan, long long nsamp,
@@ -45,15 +46,23 @@ __global__ void __launch_bounds__(kDdThreads) k_dedisperse(const float* __restri
     for (int j = 0; j < kDdD; j++)
 #pragma unroll
         for (int k = 0; k < kDdPer; k++) acc[j][k] = 0.f;
-    // dtab row c: the delays of channel c for DM trials [8 tile, 8 tile + 8)
-    // as two int4 (padding trials have delay 0 and are not summed)
-    const int4* __restrict__ dt = dtab + 2LL * tile;
-    const long long dstride = 2LL * ndtile;
+    // dtab row c: the delays of channel c for the tile's kDdD DM trials as
+    // kDdD/4 int4 (padding trials have delay 0 and are not summed)
+    constexpr int kQ = kDdD / 4;
+    const int4* __restrict__ dt = dtab + (long long)kQ * tile;
+    const long long dstride = (long long)kQ * ndtile;
 #pragma unroll 4
     for (int c = 0; c < nchan; c++) {
         const float* __restrict__ row = in + (long long)c * nsamp;
-        const int4 lo = __ldg(dt + c * dstride), hi = __ldg(dt + c * dstride + 1);
-        const int dl[kDdD] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        int dl[kDdD];
+#pragma unroll
+        for (int q = 0; q < kQ; q++) {
+            const int4 v = __ldg(dt + c * dstride + q);
+            dl[4 * q] = v.x;
+            dl[4 * q + 1] = v.y;
+            dl[4 * q + 2] = v.z;
+            dl[4 * q + 3] = v.w;
+        }
 #pragma unroll
         for (int j = 0; j < kDdD; j++) {
             if (j < nd) {  // uniform over the CTA
