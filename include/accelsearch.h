@@ -276,14 +276,17 @@ int  accel_bank_spectra(const accel_ctx *ctx, int h, accel_complex *kstd, accel_
 
 /* ------------------------------------------------------------------ serving */
 /* A request server with continuous batching (no counterpart in the
- * reference, whose driver searches one trial per process run).  A worker
- * thread admits requests in arrival order while their device memory (series
- * and spectrum, 12 bytes per sample) fits hbm_budget_bytes, transforms and
- * whitens them, and fills each launch group with the next steps of every
- * active request of one template bank (one bank per zmax, built on first
- * use), round-robin: a request admitted while others are in flight is
- * searched alongside them from the next group on.  A request's candidates
- * do not depend on what it was batched with. */
+ * reference, whose driver searches one trial per process run).  Planner
+ * threads make each request's R2C plan when it is submitted; a worker
+ * thread admits requests in arrival order, as their plans are ready, while
+ * their device memory (series and spectrum, 12 bytes per sample) fits
+ * hbm_budget_bytes, transforms and whitens them, and fills each launch
+ * group from one template bank (one bank per zmax, built on first use),
+ * shortest remaining work first: a request admitted while others are in
+ * flight joins the next group with room, and a short request overtakes a
+ * long one.  The next group is launched before the previous one's
+ * candidates are read back.  A request's candidates do not depend on what
+ * it was batched with. */
 typedef struct accel_server accel_server;
 
 typedef struct accel_server_config {
