@@ -104,6 +104,8 @@ struct HsumArgs {
     int nstages;
     unsigned long long* err;  // bit 0: a tile's copy wait timed out
     int tile_floats;          // largest shared-memory footprint of a tile (host-proven)
+    unsigned test_extra_tx;   // 0, or (failure-detection test) bytes each tile expects
+                              // beyond its copies, so that its bounded wait runs out
 };
 
 // Fundamental plane fused with the harmonic sum (k_fund_sum).

@@ -568,6 +568,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         ha.nstages = c->nstages;
         ha.err = c->d_ncand + 1;
         ha.tile_floats = c->tile_floats;
+        ha.test_extra_tx = c->wait_test ? 16u : 0u;
         ProfScope ps(c, K_HSUM, 1, sum_stream);
         c->stats.segments += nseg;
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
@@ -961,6 +962,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->serial_sum = !c->overlap;
     t->hsum_pipelined = c->hsum_pipe;
     t->graph = c->use_graph;
+    t->wait_test = c->wait_test;
     return ACCEL_OK;
 }
 
@@ -976,6 +978,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->overlap = t->serial_sum == 0;
     c->hsum_pipe = t->hsum_pipelined != 0;
     c->use_graph = t->graph != 0;
+    c->wait_test = t->wait_test != 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaStreamSynchronize(c->stream2));

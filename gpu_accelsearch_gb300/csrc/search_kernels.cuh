@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
         const int total_rows = __shfl_sync(0xffffffffu, rincl, 31);
         if (tid == 0) {
             mbar_init(&s_bar, 1);
-            mbar_arrive_expect_tx(&s_bar, 4u * (unsigned)total_floats);
+            mbar_arrive_expect_tx(&s_bar, 4u * (unsigned)total_floats + a.test_extra_tx);
         }
         __syncwarp();
         for (int j = tid; j < total_rows; j += 32) {

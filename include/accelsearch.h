@@ -116,7 +116,13 @@ typedef struct accel_tuning {
                             /* sequence keeps its shape); 0: direct launches. */
                             /* Searches that copy series from host memory     */
                             /* always launch directly                         */
-    int reserved[1];
+    int wait_test;          /* failure-detection test, 0 in normal use: each  */
+                            /* tile of the tiled harmonic sum expects 16      */
+                            /* bytes that never arrive, so its bounded copy   */
+                            /* wait (about 33 ms) runs out, the tile sets the */
+                            /* error word and returns, and the search fails   */
+                            /* with ACCEL_ERR_CUDA; no GPU fault, the context */
+                            /* stays usable                                   */
 } accel_tuning;
 
 typedef struct accel_ctx accel_ctx;

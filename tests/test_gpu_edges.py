@@ -101,3 +101,32 @@ def test_small_banks_match_oracle(zmax, numharm):
         g = _keys(gpu, 16, s.uselen // 2, -zmax)
         assert len(g) > 20
         assert _keys(hi, 0, 0, 0) <= g <= _keys(lo, 0, 0, 0)
+
+
+def test_tile_wait_timeout_reported_and_context_recovers():
+    # failure detection without a GPU fault: with tuning.wait_test every tile
+    # of the harmonic sum waits for 16 bytes that never arrive, so its bounded
+    # wait runs out, it sets the error word and returns; the search (host-fed,
+    # and from device series through the CUDA graph) fails with
+    # ACCEL_ERR_CUDA, and the same context then searches normally
+    from gpu_accelsearch_gb300.native import AccelError
+    from gpu_accelsearch_gb300.search import AccelSearch
+    n = 1 << 16
+    x = synth_series(n, seed=9, signals=[(0.3, 5000.25, 20.0)])
+    xd = torch.from_numpy(x.copy()).cuda()
+    with AccelSearch(zmax=50, numharm=4, fftlen=2048) as s:
+        s.set_tuning(hsum_pipelined=0, hsum_rowwise=0, wait_test=0)
+        s.search([x], DT)
+        want = s.candidates()
+        assert len(want) > 0
+        s.set_tuning(wait_test=1)
+        for kw in ({}, {"on_device": True, "nsamples": [n]}):
+            src = [xd.data_ptr()] if kw else [x]
+            with pytest.raises(AccelError) as e:
+                s.search(src, DT, **kw)
+            assert e.value.code == -2 and "timed out" in str(e.value)
+        s.set_tuning(wait_test=0)
+        s.search([x], DT)
+        assert np.array_equal(s.candidates(), want)
+        s.search([xd.data_ptr()], DT, on_device=True, nsamples=[n])
+        assert np.array_equal(s.candidates(), want)
