@@ -64,6 +64,10 @@ SIGNATURES = {
                                         C.POINTER(_us), C.POINTER(_us), C.c_int]),
     "initialize_cuda_plans": (None, [_us, C.POINTER(SubharmonicInfo)]),
     "free_cuda_plans": (None, [_us]),
+    "convolveSignal": (None, [C.c_int, C.c_int, _c64p, _c64p, C.c_int, _c64p]),
+    "generatePowers": (None, [C.c_int, C.c_int, C.c_int, _c64p, C.c_float, C.c_void_p]),
+    "addPowers": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _c64p,
+                         C.c_float, C.c_void_p, C.c_int]),
     "search_ffdot_powers_n": (C.POINTER(Candidates), [C.POINTER(FfdotInfo), C.c_int, C.c_float,
                                                       C.c_longlong, _lp]),
     "search_ffdot_powers": (C.POINTER(Candidates), [C.POINTER(FfdotInfo), C.c_int, C.c_float,

@@ -715,4 +715,53 @@ Candidates* search_ffdot_powers(ffdotInfo* ffdot, int numharm, float powcut, lon
     return search_ffdot_powers_n(ffdot, numharm, powcut, numindep, &n);
 }
 
+// ---- bpd_gpu_kernels.cuh:15-17: the reference's three kernels as host
+// launchers with the same names and arguments (a __global__ symbol cannot
+// cross a C ABI): each covers the whole range its reference launch covers,
+// on the legacy default stream.
+void convolveSignal(int kernelTotalNumzs, int fftlen, accel_complex* data, accel_complex* kernels,
+                    int kernelTemplateLength, accel_complex* outputdata) {
+    (void)kernelTemplateLength;  // unused by the reference kernel as well
+    g_cs.status = ACCEL_OK;
+    const long long n = (long long)kernelTotalNumzs * fftlen;
+    if (n <= 0) return;
+    k_conv<<<grid_for(n), 256>>>(kernelTotalNumzs, fftlen, reinterpret_cast<const float2*>(data),
+                                 reinterpret_cast<const float2*>(kernels), reinterpret_cast<float2*>(outputdata));
+    if (cudaGetLastError() != cudaSuccess) fail(ACCEL_ERR_CUDA, "convolveSignal");
+}
+
+void generatePowers(int kernelTotalNumzs, int numrs, int fftlen, accel_complex* data, float scale,
+                    float* outputdata) {
+    g_cs.status = ACCEL_OK;
+    const long long n = (long long)kernelTotalNumzs * numrs;
+    if (n <= 0) return;
+    k_powers<<<grid_for(n), 256>>>(kernelTotalNumzs, numrs, fftlen, reinterpret_cast<const float2*>(data), scale,
+                                   outputdata);
+    if (cudaGetLastError() != cudaSuccess) fail(ACCEL_ERR_CUDA, "generatePowers");
+}
+
+void addPowers(int fundamental_numzs, int fundamental_numrs, int subharm_fftlen, int fundamental_zlo,
+               int subharm_zlo, int subharm_rlo, double harmonicFraction, accel_complex* data, float scale,
+               float* output_powers, int fullrlo) {
+    g_cs.status = ACCEL_OK;
+    // the kernel's index arithmetic is exact for harmonicFraction = p / 2^k
+    // (every fraction the reference's bank uses)
+    int p = -1, q = 1;
+    for (int k = 0; k <= 16 && p < 0; k++, q <<= 1) {
+        const double v = harmonicFraction * q;
+        if (v == std::floor(v) && v >= 1.0 && v <= q) p = (int)v;
+    }
+    q >>= 1;
+    if (p < 0) {
+        fail(ACCEL_ERR_INVALID, "addPowers: harmonicFraction is not p / 2^k in (0, 1]");
+        return;
+    }
+    const long long n = (long long)fundamental_numzs * fundamental_numrs;
+    if (n <= 0) return;
+    k_addpowers<<<grid_for(n), 256>>>(fundamental_numzs, fundamental_numrs, subharm_fftlen, fundamental_zlo,
+                                      subharm_zlo, subharm_rlo, p, q, reinterpret_cast<const float2*>(data), scale,
+                                      output_powers, (long long)fullrlo);
+    if (cudaGetLastError() != cudaSuccess) fail(ACCEL_ERR_CUDA, "addPowers");
+}
+
 }  // extern "C"

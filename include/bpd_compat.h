@@ -130,6 +130,21 @@ void perform_harmonic_summing(unsigned short totalHarmonics, accel_complex *devi
 void initialize_cuda_plans(unsigned short totalHarmonics, SubharmonicInfo *subharmonicInfo);
 void free_cuda_plans(unsigned short totalHarmonics);
 
+/* bpd_gpu_kernels.cuh:15-17 -- the reference's kernels as host launchers
+ * with the same names and arguments (a __global__ symbol cannot cross a C
+ * ABI; a caller that wrote name<<<grid, block>>>(args) calls name(args)).
+ * Each covers the whole range of the reference's launch, on the legacy
+ * default stream; device pointers as in the reference.  convolveSignal
+ * stops at fftlen - 1 (the reference's bound also touches element fftlen);
+ * addPowers takes harmonicFraction = p / 2^k, as the bank's fractions are. */
+void convolveSignal(int kernelTotalNumzs, int fftlen, accel_complex *data, accel_complex *kernels,
+                    int kernelTemplateLength, accel_complex *outputdata);
+void generatePowers(int kernelTotalNumzs, int numrs, int fftlen, accel_complex *data, float scale,
+                    float *outputdata);
+void addPowers(int fundamental_numzs, int fundamental_numrs, int subharm_fftlen, int fundamental_zlo,
+               int subharm_zlo, int subharm_rlo, double harmonicFraction, accel_complex *data, float scale,
+               float *output_powers, int fullrlo);
+
 /* bpd_candidates.cuh:40 (a stub in the reference).  Here: the cells of the
  * power plane left by the last perform_harmonic_summing (or, before any
  * summing, generate_fundamental_powers) whose power exceeds powcut, as a

@@ -113,6 +113,72 @@ def test_reference_step_sequence(L):
     L.accel_compat_set_uselen(32000)
 
 
+def test_reference_kernel_launchers(L):
+    # convolveSignal / generatePowers / addPowers (bpd_gpu_kernels.cuh:15-17)
+    # called as the reference's stage functions call them give exactly the
+    # stage functions' outputs
+    from gpu_accelsearch_gb300 import compat as CP
+    zmax, stages, U, n = 50, 3, 1914, 1 << 18
+    L.accel_compat_set_uselen(U)
+    shi = L.createSubharmonicInfo(stages, zmax)
+    nh = L.getTotalHarmonics(stages)
+    x = synth_series(n, seed=1019, signals=[(0.05, 20000.25, 40.0)])
+    w = O.deredden(np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2])
+    starts = (C.c_long * nh)()
+    conv_idx = (C.c_long * nh)()
+    tot = tot_conv = 0
+    for h in range(nh):
+        starts[h], conv_idx[h] = tot, tot_conv
+        tot += shi[h].kernelFFTLength
+        tot_conv += shi[h].kernelFFTLength * shi[h].totalKernelsTemplates
+    L.initialize_cuda_plans(nh, shi)
+    d_data = torch.zeros(2 * tot, dtype=torch.float32, device="cuda")
+    d_fft = torch.zeros_like(d_data)
+    d_conv, d_conv2 = (torch.zeros(2 * tot_conv, dtype=torch.float32, device="cuda") for _ in range(2))
+    d_ifft = torch.zeros_like(d_conv)
+    nz0 = shi[0].totalKernelsTemplates
+    d_pow, d_pow2 = (torch.zeros(nz0 * U, dtype=torch.float32, device="cuda") for _ in range(2))
+    host = np.zeros(tot, np.complex64)
+    fi = (CP.FfdotInfo * nh)()
+    bo = (C.c_ushort * nh)()
+    startr = 16 + 20 * (U // 2)
+    L.generate_harmonics_ffdot(nh, stages, shi, startr, startr + U // 2 - 0.5, -zmax, fi, bo)
+    L.generate_harmonic_ffdot_data(nh, tot, fi, bo, starts, w.ctypes.data, w.size, 0, host.ctypes.data)
+    d_data.copy_(torch.from_numpy(host.view(np.float32)))
+    L.perform_fft_harmonics(nh, d_data.data_ptr(), starts, d_fft.data_ptr())
+    L.perform_convolution(nh, d_fft.data_ptr(), fi, shi, starts, d_conv.data_ptr(), conv_idx)
+    for h in range(nh):
+        L.convolveSignal(shi[h].totalKernelsTemplates, shi[h].kernelFFTLength,
+                         d_fft.data_ptr() + 8 * starts[h], shi[h].kernels_data, shi[h].kernelFFTLength,
+                         d_conv2.data_ptr() + 8 * conv_idx[h])
+        CP.check()
+    torch.cuda.synchronize()
+    assert torch.equal(d_conv.view(torch.int32), d_conv2.view(torch.int32))
+    L.perform_inversefft(nh, d_conv.data_ptr(), conv_idx, d_ifft.data_ptr())
+    L.generate_fundamental_powers(nh, d_ifft.data_ptr(), conv_idx, fi, shi, d_pow.data_ptr())
+    off0 = 2 * shi[0].kernelHalfWidth[0]
+    L.generatePowers(fi[0].numzs, fi[0].numrs, fi[0].fftlen, d_ifft.data_ptr() + 8 * (conv_idx[0] + off0),
+                     float(np.float32(1.0 / (fi[0].fftlen * fi[0].fftlen))), d_pow2.data_ptr())
+    CP.check()
+    torch.cuda.synchronize()
+    assert torch.equal(d_pow.view(torch.int32), d_pow2.view(torch.int32))
+    L.perform_harmonic_summing(nh, d_ifft.data_ptr(), conv_idx, fi, shi, d_pow.data_ptr(), int(startr),
+                               None, None, 0)
+    for h in range(1, nh):
+        off = 2 * shi[h].kernelHalfWidth[0]
+        L.addPowers(fi[0].numzs, fi[0].numrs, fi[h].fftlen, fi[0].zlo, fi[h].zlo, fi[h].rlo,
+                    fi[h].currentHarmonic / fi[h].maxHarmonic, d_ifft.data_ptr() + 8 * (conv_idx[h] + off),
+                    float(np.float32(1.0 / (fi[h].fftlen * fi[h].fftlen))), d_pow2.data_ptr(), int(startr))
+        CP.check()
+    torch.cuda.synchronize()
+    assert torch.equal(d_pow.view(torch.int32), d_pow2.view(torch.int32))
+    L.addPowers(1, 1, 2048, 0, 0, 0, 1.0 / 3.0, d_ifft.data_ptr(), 1.0, d_pow2.data_ptr(), 0)
+    assert L.accel_compat_status() == -1  # not p / 2^k
+    L.free_cuda_plans(nh)
+    L.freeSubharmonicInfo(shi, nh)
+    L.accel_compat_set_uselen(32000)
+
+
 @pytest.mark.parametrize("length,batch", [(2048, 3), (16384, 2), (32768, 1)])
 def test_c2c_transforms(L, length, batch):
     rng = np.random.default_rng(length)
