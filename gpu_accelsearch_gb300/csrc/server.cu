@@ -1,9 +1,10 @@
 // server.cu -- continuous-batching request server (accel_server_*).
 //
 // Requests are single DM-trial time series.  A scheduler thread
-//   * admits queued requests in arrival order while their device memory
-//     (series + spectrum) fits the HBM budget and the active limit, copies
-//     the series in, and runs the R2C transform and whitening on the device;
+//   * admits queued requests in arrival order, as their R2C plans are
+//     ready, while their device memory (series + spectrum) fits the HBM
+//     budget and the active limit, copies the series in, and runs the R2C
+//     transform and whitening on the device;
 //   * builds each launch group from the active requests of one template
 //     bank (one bank per zmax, created on first use), shortest remaining
 //     work first: the bank holding the active request with the least work
@@ -12,9 +13,11 @@
 //     others are in flight joins the very next group that has room, so its
 //     work overlaps with theirs on the device, and a short request overtakes
 //     a long one instead of sharing the GPU with it step by step;
-//   * completes a request when its last step has been summed: candidates
-//     are kept for accel_server_result, its device memory is released and
-//     its latency (submission to completion) recorded.
+//   * launches the next group before it reads back the previous one (two
+//     buffer sets per bank), and completes a request when its last step
+//     has been summed: candidates are kept for accel_server_result, its
+//     device memory is released and its latency (submission to completion)
+//     recorded.
 // Each segment is computed independently of the others in its group, so a
 // request's result does not depend on what it was batched with.
 //
