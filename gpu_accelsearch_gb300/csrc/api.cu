@@ -908,8 +908,10 @@ int accel_destroy(accel_ctx* c) {
 
 int accel_set_stream(accel_ctx* c, void* s) {
     if (!c) return set_err(ACCEL_ERR_INVALID, "null context");
+    // work already issued on the old stream finishes first: buffers it uses
+    // may be freed in stream order on the new one (whitening-plan eviction)
+    if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->own_stream && c->stream) {
-        cudaStreamSynchronize(c->stream);
         cudaStreamDestroy(c->stream);
         c->own_stream = false;
         c->stream = nullptr;

@@ -134,7 +134,8 @@ void accel_config_init(accel_config *cfg);
 int  accel_create(const accel_config *cfg, accel_ctx **out);
 int  accel_destroy(accel_ctx *ctx);
 /* Run all further work of ctx on this cudaStream_t (NULL: the context's own,
- * a blocking stream ordered with the legacy default stream). */
+ * a blocking stream ordered with the legacy default stream).  Waits for the
+ * work already issued on the previous stream. */
 int  accel_set_stream(accel_ctx *ctx, void *cuda_stream);
 int  accel_synchronize(accel_ctx *ctx);
 /* Time every kernel with CUDA events on the context's stream (1) or not (0). */
