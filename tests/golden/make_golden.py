@@ -127,6 +127,17 @@ def main():
     L.ref_deredden(fp(w.view(np.float32)), w.size)
     pins["deredden"] = {"numbins": int(spec.size), "seed": 11, "in_sha": sha(spec),
                         "out_sha": sha(w), "head": w.view(np.float32)[:16].tolist()}
+    # short spectra whose last block slope drives the extrapolated tail level
+    # below zero (5220 bins: NaN at the end) beside ordinary ones
+    tails = []
+    for numbins in (3000, 4184, 5220):
+        spec = synth_red_spectrum(numbins + 1, seed=numbins)[:numbins]
+        w = spec.copy()
+        L.ref_deredden(fp(w.view(np.float32)), w.size)
+        f = w.view(np.float32)
+        tails.append({"numbins": numbins, "seed": numbins, "in_sha": sha(spec), "out_sha": sha(w),
+                      "nan_floats": np.nonzero(np.isnan(f))[0].tolist()})
+    pins["deredden_tails"] = tails
 
     # banks: geometry + time-domain templates
     banks = []

@@ -67,6 +67,21 @@ def test_deredden(pins):
     assert sha(O.deredden(spec)) == rec["out_sha"]
 
 
+def test_deredden_short_spectra_and_nan_tail(pins):
+    # the reference's whitening of short spectra; at 5220 bins the last
+    # slope drives the extrapolated tail level below zero and the reference
+    # itself gives NaN there (the oracle and the GPU follow it)
+    for rec in pins["deredden_tails"]:
+        n = rec["numbins"]
+        spec = synth_red_spectrum(n + 1, seed=rec["seed"])[:n]
+        assert sha(spec) == rec["in_sha"], "synthetic generator changed"
+        w = O.deredden(spec)
+        f = w.view(np.float32)
+        assert np.nonzero(np.isnan(f))[0].tolist() == rec["nan_floats"]
+        assert sha(w) == rec["out_sha"], n
+    assert any(rec["nan_floats"] for rec in pins["deredden_tails"])
+
+
 @pytest.mark.parametrize("bank_index", range(7))
 def test_bank(pins, bank_index):
     rec = pins["banks"][bank_index]
