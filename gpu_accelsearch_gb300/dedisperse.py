@@ -34,6 +34,22 @@ def dedisperse(filterbank_dev: int, nchan: int, nsamp: int, delays: np.ndarray, 
                                      nout, stream or None))
 
 
+def read_filterbank(path: str):
+    """(header dict, float32[nchans][nsamples]) of a SIGPROC filterbank file
+    (accel_read_filterbank): channel-major, channel c at fch1 + c * foff MHz."""
+    info = N.FilterbankInfo()
+    ptr = C.POINTER(C.c_float)()
+    N.check(N.lib().accel_read_filterbank(str(path).encode(), C.byref(info), C.byref(ptr)))
+    try:
+        n = info.nchans * info.nsamples
+        data = np.ctypeslib.as_array(ptr, shape=(n,)).copy().reshape(info.nchans, info.nsamples)
+    finally:
+        N.lib().accel_free_host(ptr)
+    hdr = {f: getattr(info, f) for f, _ in info._fields_}
+    hdr["source_name"] = info.source_name.decode(errors="replace")
+    return hdr, data
+
+
 def _main(argv=None) -> None:
     """Time one dedispersion of a seeded N(0,1) filterbank on cuda:0:
     python -m gpu_accelsearch_gb300.dedisperse --nchan 256 --nout 262144 --ndm 64"""

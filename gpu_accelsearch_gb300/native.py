@@ -67,6 +67,12 @@ class Optimized(C.Structure):
                 ("period", C.c_double), ("pdot", C.c_double)]
 
 
+class FilterbankInfo(C.Structure):
+    _fields_ = [("nchans", C.c_int), ("nbits", C.c_int), ("nifs", C.c_int), ("nsamples", C.c_longlong),
+                ("tsamp", C.c_double), ("fch1", C.c_double), ("foff", C.c_double),
+                ("tstart", C.c_double), ("source_name", C.c_char * 80), ("header_bytes", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 6),
                 ("kind_ms", C.c_double * 6), ("segments", C.c_longlong),
@@ -139,6 +145,9 @@ SIGNATURES = {
                                           C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int)]),
     "accel_dedisperse": (C.c_int, [_vp, C.c_int, _ll, C.POINTER(C.c_int), C.c_int, _vp, _ll, _vp]),
+    "accel_read_filterbank": (C.c_int, [C.c_char_p, C.POINTER(FilterbankInfo),
+                                        C.POINTER(C.POINTER(C.c_float))]),
+    "accel_free_host": (None, [_vp]),
 }
 
 _lib = None

@@ -355,6 +355,24 @@ int  accel_dedisperse_delays(int nchan, double f_top_mhz, double chan_bw_mhz, do
 int  accel_dedisperse(const float *filterbank_dev, int nchan, long long nsamp, const int *delays,
                       int ndm, float *out_dev, long long nout, void *cuda_stream);
 
+/* SIGPROC filterbank reader (host only; the reference reads dedispersed
+ * .dat series only, bpd_data.c:9-75, and no function of it is replaced):
+ * the header keywords, then nifs = 1 time-major samples of 8 or 16 bits
+ * (unsigned) or 32 bits (float).  *data is a malloc'd float32
+ * [nchans][nsamples], channel-major as accel_dedisperse takes it (channel c
+ * at fch1 + c * foff MHz); free it with accel_free_host. */
+typedef struct accel_filterbank_info {
+    int nchans, nbits, nifs;
+    long long nsamples;
+    double tsamp;           /* seconds                                        */
+    double fch1, foff;      /* MHz: first channel, channel step               */
+    double tstart;          /* MJD                                            */
+    char source_name[80];
+    int header_bytes;
+} accel_filterbank_info;
+int  accel_read_filterbank(const char *path, accel_filterbank_info *info, float **data);
+void accel_free_host(void *p);
+
 #ifdef __cplusplus
 }
 #endif

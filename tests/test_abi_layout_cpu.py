@@ -18,6 +18,7 @@ STRUCTS = [("accel_config", N.Config), ("accel_harmonic", N.Harmonic),
            ("accel_candidate", N.Candidate), ("accel_stats", N.Stats),
            ("accel_tuning", N.Tuning), ("accel_optimized", N.Optimized),
            ("accel_server_config", N.ServerConfig), ("accel_server_stats", N.ServerStats),
+           ("accel_filterbank_info", N.FilterbankInfo),
            ("SubharmonicInfo", CP.SubharmonicInfo), ("ffdotInfo", CP.FfdotInfo),
            ("Candidates", CP.Candidates)]
 
