@@ -262,7 +262,7 @@ def precision_report(seeds: int, device: int):
     U, half = s32.uselen, s32.uselen // 2
     rec16 = rec32 = inj = 0
     agree = tot32 = 0
-    worst_err, errs = 0.0, []
+    worst_err, err_sum, err_cells = 0.0, 0.0, 0
     orc = None
     for seed in range(seeds):
         rng = np.random.default_rng(9000 + seed)
@@ -290,38 +290,49 @@ def precision_report(seeds: int, device: int):
                     rec32 += int(hit)
                 else:
                     rec16 += int(hit)
-        if seed < 2:  # power error against the FP64 oracle on the step holding the first signal
-            if orc is None:
-                orc = O.Oracle(ZMAX, NUMHARM, U)
-            spec = torch.fft.rfft(x.double()).to(torch.complex64)[: n // 2].cpu().numpy()
-            w = O.deredden(spec)
-            rlo = int(np.floor(np.float32(n) * np.float32(DT)))
-            step = max(0, int((sigs[0][1] + sigs[0][2] / 2 - rlo) // half) - 1)
-            startr = rlo + step * half
-            d = torch.from_numpy(w.view(np.float32).copy()).cuda()
-            dh = torch.zeros(s16.dhalf_stride * 2, dtype=torch.float32, device="cuda")
-            pl = torch.zeros(s16.plane_stride, dtype=torch.float32, device="cuda")
-            s16.prepare_segments(d.data_ptr(), w.size, [startr], dh.data_ptr())
-            s16.power_planes(dh.data_ptr(), 1, pl.data_ptr())
-            P = pl.cpu().numpy()
-            for h, hi in enumerate(s16.harmonics):
-                p64 = orc.harmonic_plane(w, float(startr), h)
-                nz, nr = p64.shape
-                g = P[s16.plane_off[h]: s16.plane_off[h] + nz * s16.plane_row[h]].reshape(
-                    nz, s16.plane_row[h])[:, :nr]
-                e = np.abs(g - p64) / np.maximum(p64, 1.0)
-                worst_err = max(worst_err, float(e.max()))
-                errs.append(float(e.mean()))
+        # power error against the FP64 oracle on the step holding the first signal
+        if orc is None:
+            orc = O.Oracle(ZMAX, NUMHARM, U)
+            from concurrent.futures import ThreadPoolExecutor
+            pool = ThreadPoolExecutor(max_workers=len(s16.harmonics))
+        spec = torch.fft.rfft(x.double()).to(torch.complex64)[: n // 2].cpu().numpy()
+        w = O.deredden(spec)
+        rlo = int(np.floor(np.float32(n) * np.float32(DT)))
+        step = max(0, int((sigs[0][1] + sigs[0][2] / 2 - rlo) // half))
+        startr = rlo + step * half
+        d = torch.from_numpy(w.view(np.float32).copy()).cuda()
+        dh = torch.zeros(s16.dhalf_stride * 2, dtype=torch.float32, device="cuda")
+        pl = torch.zeros(s16.plane_stride, dtype=torch.float32, device="cuda")
+        s16.prepare_segments(d.data_ptr(), w.size, [startr], dh.data_ptr())
+        s16.power_planes(dh.data_ptr(), 1, pl.data_ptr())
+        P = pl.cpu().numpy()
+        # the oracle's planes of the eight harmonics in parallel (the C
+        # calls release the interpreter lock)
+        p64s = list(pool.map(lambda h: orc.harmonic_plane(w, float(startr), h),
+                             range(len(s16.harmonics))))
+        for h, hi in enumerate(s16.harmonics):
+            p64 = p64s[h]
+            nz, nr = p64.shape
+            g = P[s16.plane_off[h]: s16.plane_off[h] + nz * s16.plane_row[h]].reshape(
+                nz, s16.plane_row[h])[:, :nr]
+            e = np.abs(g - p64) / np.maximum(p64, 1.0)
+            worst_err = max(worst_err, float(e.max()))
+            err_sum += float(e.sum())
+            err_cells += e.size
     s32.close()
     s16.close()
     if orc is not None:
+        pool.shutdown()
         orc.close()
     return {"seeds": seeds, "injected": inj, "recovered_fp32": rec32, "recovered_fp16": rec16,
             "recovery_rate_fp16": rec16 / max(inj, 1), "recovery_rate_fp32": rec32 / max(inj, 1),
             "candidate_agreement_fp16_vs_fp32": agree / max(tot32, 1),
             "max_rel_power_error_vs_fp64": worst_err,
-            "mean_rel_power_error_vs_fp64": float(np.mean(errs)) if errs else None,
-            "error_metric": "|P - P64| / max(P64, 1) over every plane of one step per seed (2 seeds)",
+            "mean_rel_power_error_vs_fp64": err_sum / err_cells if err_cells else None,
+            "error_cells": err_cells,
+            "error_metric": f"|P - P64| / max(P64, 1) over every cell of every plane of the step "
+                            f"holding the first signal, for each of the {seeds} seeds (max, and mean "
+                            "over all those cells)",
             "workload": "N=2^22, 3 injected signals per seed, zmax=200, 8 harmonics, L=8192, sigma=6"}
 
 
@@ -473,7 +484,9 @@ def run_ours(args):
     el = float(el_t.item())
     value = cells * args.steps * world / el
 
-    # ---- e2e: pinned host series through the C ABI
+    # ---- e2e: pinned host series through the C ABI, host wall clock from
+    # the call to its return (copies in, search, candidate read-back and the
+    # host's conversion and sort of the candidate list)
     e2e = None
     if not args.no_e2e:
         host = [x.cpu().pin_memory() for x in series]
@@ -485,37 +498,59 @@ def run_ours(args):
         nc = 0
         clk2 = Clocks(local)
         clk2.start()
+        t2 = time.perf_counter()
         for _ in range(args.steps):
             nc = s.search_ptrs(hptrs, lengths, DT, on_device=False)
         torch.cuda.synchronize()
+        wall2 = time.perf_counter() - t2
         clocks_e2e = clk2.stop()
-        el2 = s.stats()["search_ms"] / 1e3
+        dev2 = s.stats()["search_ms"] / 1e3
         barrier()
-        el2_t = torch.tensor([el2], device="cuda")
+        el2_t = torch.tensor([wall2, dev2], device="cuda")
         if world > 1:
             dist.all_reduce(el2_t, op=dist.ReduceOp.MAX)
-        e2e = {"value": cells * args.steps * world / float(el2_t.item()), "unit": "cells/s",
+        wall2, dev2 = float(el2_t[0].item()), float(el2_t[1].item())
+        e2e = {"value": cells * args.steps * world / wall2, "unit": "cells/s",
                "h2d_bytes_per_step": int(sum(lengths) * 4),
-               "d2h_bytes_per_step": int(8 + 16 * nc), "clocks": clocks_e2e}
+               "d2h_bytes_per_step": int(16 + 16 * nc),
+               "timing": "host wall clock around accel_search (pinned host series in, candidate "
+                         "list out, host conversion and sort included); max over ranks",
+               "wall_ms_per_step": 1e3 * wall2 / args.steps,
+               "device_event_ms_per_step": 1e3 * dev2 / args.steps,
+               "clocks": clocks_e2e}
 
-    # ---- plain per-trial path: one 2^22 trial, one step per launch group
-    plain = None
+    # ---- plain per-trial path, two ways: (a) the reference's control flow,
+    # one overlap-save step per launch group, one 2^22 trial; (b) one 2^22
+    # trial per search at the tuned launch-group size and layout -- what
+    # batching across trials adds beyond filling the launch groups
+    plain = plain_trial = None
     if not args.no_plain and rank == 0:
-        p = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=1, device=local)
         xs = device_series(torch, [1 << 22], [None], seed=7)
-        pn = p.step_count(1 << 22, DT)
-        p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
-        torch.cuda.synchronize()
-        p.reset_stats()
-        reps = 3
-        for _ in range(reps):
-            p.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
-        torch.cuda.synchronize()
-        pel = p.stats()["search_ms"] / 1e3
-        plain = {"value": pn * p.uselen * p.harmonics[0].numzs * reps / pel, "unit": "cells/s",
-                 "workload": "one 2^22-sample trial, one overlap-save step per launch group "
-                             f"({pn} steps)"}
+
+        def time_trial(search, reps=3):
+            search.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
+            torch.cuda.synchronize()
+            search.reset_stats()
+            for _ in range(reps):
+                search.search([xs[0].data_ptr()], DT, on_device=True, nsamples=[1 << 22])
+            torch.cuda.synchronize()
+            n1 = search.step_count(1 << 22, DT)
+            return n1, n1 * search.uselen * search.harmonics[0].numzs * reps / (search.stats()["search_ms"] / 1e3)
+
+        p = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=1, device=local)
+        pn, pv = time_trial(p)
         p.close()
+        plain = {"value": pv, "unit": "cells/s",
+                 "workload": "one 2^22-sample trial, one overlap-save step per launch group "
+                             f"({pn} steps, L={FFTLEN}): the reference's step-at-a-time control flow"}
+        q = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local)
+        q.set_tuning(chunk_segments=chunk, plane_split=split, **extra)
+        qn, qv = time_trial(q)
+        q.close()
+        plain_trial = {"value": qv, "unit": "cells/s",
+                       "workload": f"one 2^22-sample trial per search ({qn} steps), launch groups of "
+                                   f"{chunk} segments, L={fftlen}: the batched search's own launch "
+                                   "shape on a single trial"}
 
     if rank != 0:
         s.close()
@@ -610,6 +645,8 @@ def run_ours(args):
         "cpu_baseline": cb, "e2e": e2e, "gpu_launches": st["launches"], "clocks": clocks,
         "plain": plain,
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
+        "plain_per_trial": plain_trial,
+        "batched_over_plain_per_trial": (value / world / plain_trial["value"]) if plain_trial else None,
         "candidates_per_step": ncand,
         "serving": serving, "serving_half_load": serving_half, "dedisperse": dedisp,
         "precision_fp16": precision,

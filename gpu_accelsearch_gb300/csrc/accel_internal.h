@@ -10,6 +10,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <utility>
+#include <vector>
 
 #include "accel_common.cuh"
 
@@ -189,5 +191,14 @@ int set_error(int code, const char* fmt, ...);
 struct WhitenPlan;
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
                   unsigned numbins, int maxlen, cudaStream_t st, int exact_rsqrt = 0);
+// Largest spectrum the whitening takes: block starts and lengths are int
+// (as in the reference's recurrence) and every block lies below numbins.
+constexpr long long kMaxWhitenBins = 0x7fffffffLL;
+// Block recurrence of deredden (bpd_noise.c:33-79) in 64-bit arithmetic:
+// writes the first min(count, cap) blocks to start/len (either may be null
+// when cap is 0) and returns the number of blocks, or -1 when numbins,
+// initbuf or maxbuf is out of range.
+long long whiten_blocks(long long numbins, int initbuf, int maxbuf, int* start, int* len, long long cap);
+std::vector<std::pair<int, int>> plan_whiten_blocks(long long numbins, int initbuf, int maxbuf);
 
 }  // namespace accel

@@ -98,24 +98,6 @@ double sigma_of_power(double power, int numharm, double numindep) {
 }
 }  // namespace
 
-namespace accel {
-// Serial block recurrence of deredden (bpd_noise.c:33-79).
-std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbuf, int maxbuf) {
-    std::vector<std::pair<int, int>> b;
-    int binnum = 1, buflen = initbuf;
-    b.push_back({binnum, buflen});
-    binnum += buflen;
-    buflen = (int)(initbuf * std::log((double)binnum));
-    if (buflen > maxbuf) buflen = maxbuf;
-    while ((unsigned)(binnum + buflen) < numbins) {
-        b.push_back({binnum, buflen});
-        binnum += buflen;
-        buflen = (int)(initbuf * std::log((double)binnum));
-        if (buflen > maxbuf) buflen = maxbuf;
-    }
-    return b;
-}
-}  // namespace accel
 
 
 namespace accel {
@@ -398,6 +380,9 @@ int whiten_plan(accel_ctx* c, unsigned numbins, WhitenPlanDev** out) {
     }
     if (numbins <= (unsigned)(1 + c->cfg.whiten_initbuf))
         return set_err(ACCEL_ERR_INVALID, "spectrum of %u bins is too short to whiten", numbins);
+    if ((long long)numbins > kMaxWhitenBins)
+        return set_err(ACCEL_ERR_INVALID, "spectrum of %u bins exceeds the whitening limit of %lld", numbins,
+                       kMaxWhitenBins);
     if (c->wplans.size() >= kWhitenPlans) {
         auto lru = c->wplans.begin();
         for (auto e = c->wplans.begin(); e != c->wplans.end(); ++e)
@@ -1080,10 +1065,24 @@ int accel_harmonic_indices(long long startr, int uselen, int harmnum, int maxhar
 }
 
 int accel_whiten(accel_ctx* c, accel_complex* spec, long long numbins) {
-    if (!c || !spec || numbins <= 0 || numbins > 0xffffffffLL) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    if (!c || !spec || numbins <= 0) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    if (numbins > kMaxWhitenBins)
+        return set_err(ACCEL_ERR_INVALID, "accel_whiten: %lld bins exceed the limit of %lld", numbins,
+                       kMaxWhitenBins);
     int rc = ensure_device(c);
     if (rc) return rc;
     return do_whiten(c, reinterpret_cast<float2*>(spec), (unsigned)numbins);
+}
+
+int accel_whiten_blocks(long long numbins, int initbuf, int maxbuf, int* start, int* len, long long cap,
+                        long long* nblocks) {
+    if (!nblocks || cap < 0 || (cap > 0 && (!start || !len))) return set_err(ACCEL_ERR_INVALID, "bad argument");
+    const long long n = whiten_blocks(numbins, initbuf, maxbuf, start, len, cap);
+    if (n < 0)
+        return set_err(ACCEL_ERR_INVALID, "accel_whiten_blocks: %lld bins or widths %d/%d out of range", numbins,
+                       initbuf, maxbuf);
+    *nblocks = n;
+    return ACCEL_OK;
 }
 
 int accel_rfft(accel_ctx* c, const float* series, long long n, accel_complex* spec) {

@@ -197,9 +197,6 @@ float rsqrt_magic_host(float x) {
 
 }  // namespace
 
-// Serial whitening block plan shared with the context path (api.cu).
-std::vector<std::pair<int, int>> plan_whiten_blocks(unsigned numbins, int initbuf, int maxbuf);
-
 }  // namespace accel
 
 using namespace accel;
@@ -438,8 +435,8 @@ unsigned inverseComplexToComplexFFT(accel_complex* din, unsigned int L, accel_co
 
 void deredden(accel_complex* fft, unsigned numbins) {
     g_cs.status = ACCEL_OK;
-    if (!fft || numbins < 8) {
-        fail(ACCEL_ERR_INVALID, "deredden: bad argument");
+    if (!fft || numbins < 8 || (long long)numbins > kMaxWhitenBins) {
+        fail(ACCEL_ERR_INVALID, "deredden: bad argument (numbins must be in [8, 2^31 - 1])");
         return;
     }
     auto blocks = plan_whiten_blocks(numbins, 6, 200);  // bpd_noise.c:14 widths

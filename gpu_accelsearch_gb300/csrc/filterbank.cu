@@ -6,8 +6,10 @@
 // Format (SIGPROC): a header of keywords, each an int32 byte count and that
 // many characters, between HEADER_START and HEADER_END; a keyword is
 // followed by its value (int32, float64 or a counted string, by keyword).
-// Then the samples, time-major: for every time sample nifs x nchans values
-// of nbits bits (8 and 16: unsigned integers, 32: float32).  The reader
+// The keyword "signed" takes a single byte (nonzero: 8-bit samples are
+// two's-complement, as some writers mark them).  Then the samples,
+// time-major: for every time sample nifs x nchans values of nbits bits (8:
+// unsigned, or signed where the header says so; 16: unsigned; 32: float32).  The reader
 // returns them channel-major, float32 [nchans][nsamples], the layout
 // accel_dedisperse takes; channel c is at fch1 + c * foff MHz.
 #include <algorithm>
@@ -23,7 +25,7 @@
 
 namespace {
 
-enum Kind { K_INT, K_DBL, K_STR, K_NONE };
+enum Kind { K_INT, K_DBL, K_STR, K_BYTE, K_NONE };
 
 Kind keyword_kind(const std::string& k) {
     static const char* ints[] = {"telescope_id", "machine_id", "data_type", "barycentric", "pulsarcentric",
@@ -37,6 +39,7 @@ Kind keyword_kind(const std::string& k) {
         if (k == s) return K_DBL;
     for (const char* s : strs)
         if (k == s) return K_STR;
+    if (k == "signed") return K_BYTE;
     return K_NONE;
 }
 
@@ -91,6 +94,11 @@ int accel_read_filterbank(const char* path, accel_filterbank_info* info, float**
             else if (key == "fch1") info->fch1 = v;
             else if (key == "foff") info->foff = v;
             else if (key == "tstart") info->tstart = v;
+        } else if (kind == K_BYTE) {
+            unsigned char v;
+            if (fread(&v, 1, 1, fb.f) != 1)
+                return accel::set_error(ACCEL_ERR_INVALID, "accel_read_filterbank: truncated header");
+            info->is_signed = v != 0;
         } else if (kind == K_STR) {
             std::string v;
             if (!read_string(fb.f, &v))
@@ -136,7 +144,7 @@ int accel_read_filterbank(const char* path, accel_filterbank_info* info, float**
             for (int c = 0; c < nc; c++) {
                 float v;
                 if (info->nbits == 8) {
-                    v = (float)p[c];
+                    v = info->is_signed ? (float)(int)(signed char)p[c] : (float)p[c];
                 } else if (info->nbits == 16) {
                     uint16_t u;
                     std::memcpy(&u, p + 2 * c, 2);

@@ -209,6 +209,44 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_whiten_scale_warp(const i
     }
 }
 
+// Block recurrence of deredden (bpd_noise.c:33-79): the first block holds
+// initbuf bins from bin 1; each next block starts where the last ended and
+// holds (int)(initbuf * ln(start)) bins, at most maxbuf; blocks continue
+// while start + length < numbins.  Positions are carried in 64 bits so that
+// no sum overflows near kMaxWhitenBins; the width is clamped before the
+// conversion to int (same result wherever the reference's is defined).
+long long whiten_blocks(long long numbins, int initbuf, int maxbuf, int* start, int* len, long long cap) {
+    if (initbuf < 1 || maxbuf < 1 || numbins <= 1 + (long long)initbuf || numbins > kMaxWhitenBins) return -1;
+    auto width = [&](long long at) {
+        const double x = initbuf * std::log((double)at);
+        return x >= (double)maxbuf ? maxbuf : (int)x;
+    };
+    long long n = 0, binnum = 1;
+    int buflen = initbuf;
+    for (;;) {
+        if (n < cap) {
+            start[n] = (int)binnum;
+            len[n] = buflen;
+        }
+        n++;
+        binnum += buflen;
+        buflen = width(binnum);
+        if (binnum + buflen >= numbins) break;
+    }
+    return n;
+}
+
+std::vector<std::pair<int, int>> plan_whiten_blocks(long long numbins, int initbuf, int maxbuf) {
+    const long long n = whiten_blocks(numbins, initbuf, maxbuf, nullptr, nullptr, 0);
+    std::vector<std::pair<int, int>> b;
+    if (n <= 0) return b;
+    std::vector<int> s((size_t)n), l((size_t)n);
+    whiten_blocks(numbins, initbuf, maxbuf, s.data(), l.data(), n);
+    b.reserve((size_t)n);
+    for (long long i = 0; i < n; i++) b.push_back({s[i], l[i]});
+    return b;
+}
+
 int launch_whiten(const int* d_bstart, const int* d_blen, int nblocks, double* d_med, float2* spec,
                   unsigned numbins, int maxlen, cudaStream_t st, int exact) {
     if (maxlen <= kWarpBlockMax) {
@@ -260,26 +298,6 @@ void* g_noalloc_addr[kNoAllocDevices];           // device address of g_whiten_s
 int g_noalloc_start[kNoAllocBlocks];             // host staging of the block table
 int g_noalloc_len[kNoAllocBlocks];
 
-// The block recurrence of deredden (bpd_noise.c:33-79) into fixed arrays.
-// Returns the number of blocks, or -1 when it exceeds kNoAllocBlocks.
-int plan_blocks_fixed(unsigned numbins, int initbuf, int maxbuf) {
-    int n = 0, binnum = 1, buflen = initbuf;
-    g_noalloc_start[n] = binnum;
-    g_noalloc_len[n++] = buflen;
-    binnum += buflen;
-    buflen = (int)(initbuf * std::log((double)binnum));
-    if (buflen > maxbuf) buflen = maxbuf;
-    while ((unsigned)(binnum + buflen) < numbins) {
-        if (n >= kNoAllocBlocks) return -1;
-        g_noalloc_start[n] = binnum;
-        g_noalloc_len[n++] = buflen;
-        binnum += buflen;
-        buflen = (int)(initbuf * std::log((double)binnum));
-        if (buflen > maxbuf) buflen = maxbuf;
-    }
-    return n;
-}
-
 }  // namespace
 }  // namespace accel
 
@@ -290,14 +308,25 @@ extern "C" int accel_whiten_noalloc(accel_complex* spec, long long numbins, int 
     if (initbuf < 1 || maxbuf < 1 || maxbuf > 49152)
         return set_error(ACCEL_ERR_INVALID,
                          "accel_whiten_noalloc: block widths must be in [1, 49152]");
-    if (numbins <= 1 + (long long)initbuf || numbins > 0xffffffffLL)
-        return set_error(ACCEL_ERR_INVALID, "accel_whiten_noalloc: %lld bins out of range", numbins);
+    if (numbins <= 1 + (long long)initbuf || numbins > kMaxWhitenBins)
+        return set_error(ACCEL_ERR_INVALID, "accel_whiten_noalloc: %lld bins out of range (%d .. %lld)",
+                         numbins, initbuf + 2, kMaxWhitenBins);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return set_error(ACCEL_ERR_CUDA, "accel_whiten_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kNoAllocDevices)
         return set_error(ACCEL_ERR_UNSUPPORTED, "accel_whiten_noalloc: device %d", dev);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The block table goes to the device by a copy from host arrays that the
+    // next call overwrites: a captured copy would replay whatever table the
+    // latest call left there, so calls inside a stream capture are refused.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        if (e != cudaSuccess) cudaGetLastError();
+        return set_error(ACCEL_ERR_UNSUPPORTED, "accel_whiten_noalloc: not callable during stream capture");
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_addr[dev]) {
         // once per device, with that device current: the array's device address
@@ -308,8 +337,9 @@ extern "C" int accel_whiten_noalloc(accel_complex* spec, long long numbins, int 
                              cudaGetErrorString(e));
         g_noalloc_addr[dev] = p;
     }
-    const int nb = plan_blocks_fixed((unsigned)numbins, initbuf, maxbuf);
-    if (nb < 0)
+    const long long nbl = whiten_blocks(numbins, initbuf, maxbuf, g_noalloc_start, g_noalloc_len, kNoAllocBlocks);
+    const int nb = (int)nbl;
+    if (nbl > kNoAllocBlocks)
         return set_error(ACCEL_ERR_INVALID,
                          "accel_whiten_noalloc: %lld bins need more than %d whitening blocks, the "
                          "size of the static scratch (about 1.2e7 bins with the default widths)",
@@ -320,7 +350,6 @@ extern "C" int accel_whiten_noalloc(accel_complex* spec, long long numbins, int 
     int* d_start = reinterpret_cast<int*>(base);
     int* d_len = reinterpret_cast<int*>(base + sizeof(int) * kNoAllocBlocks);
     double* d_med = reinterpret_cast<double*>(base + 2 * sizeof(int) * kNoAllocBlocks);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     // pageable source: the copies have left the host arrays when they return
     e = cudaMemcpyAsync(d_start, g_noalloc_start, sizeof(int) * nb, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)

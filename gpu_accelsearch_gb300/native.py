@@ -70,7 +70,8 @@ class Optimized(C.Structure):
 class FilterbankInfo(C.Structure):
     _fields_ = [("nchans", C.c_int), ("nbits", C.c_int), ("nifs", C.c_int), ("nsamples", C.c_longlong),
                 ("tsamp", C.c_double), ("fch1", C.c_double), ("foff", C.c_double),
-                ("tstart", C.c_double), ("source_name", C.c_char * 80), ("header_bytes", C.c_int)]
+                ("tstart", C.c_double), ("source_name", C.c_char * 80), ("header_bytes", C.c_int),
+                ("is_signed", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -125,6 +126,8 @@ SIGNATURES = {
                                             C.c_int, C.POINTER(Optimized)]),
     "accel_trial_spectrum": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(C.c_longlong)]),
     "accel_whiten": (C.c_int, [_vp, _vp, _ll]),
+    "accel_whiten_blocks": (C.c_int, [_ll, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      _ll, _llp]),
     "accel_rfft": (C.c_int, [_vp, _vp, _ll, _vp]),
     "accel_prepare_segments": (C.c_int, [_vp, _vp, _ll, _llp, C.c_int, _vp]),
     "accel_power_planes": (C.c_int, [_vp, _vp, C.c_int, _vp]),

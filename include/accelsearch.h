@@ -240,8 +240,15 @@ int  accel_trial_spectrum(accel_ctx *ctx, int trial, const accel_complex **spec_
                           long long *numbins);
 
 /* ------------------------------------------------------------ stage calls */
-/* Whitening in place (deredden, bpd_noise.c:12-92). */
+/* Whitening in place (deredden, bpd_noise.c:12-92), numbins <= 2^31 - 1. */
 int  accel_whiten(accel_ctx *ctx, accel_complex *spec_dev, long long numbins);
+/* Host only: the whitening block plan of deredden's recurrence
+ * (bpd_noise.c:33-79) -- block k holds bins [start[k], start[k] + len[k]).
+ * Writes the first min(*nblocks, cap) blocks and sets *nblocks to the full
+ * count; ACCEL_ERR_INVALID when numbins is not in [initbuf + 2, 2^31 - 1] or
+ * a width is below 1. */
+int  accel_whiten_blocks(long long numbins, int initbuf, int maxbuf, int *start, int *len,
+                         long long cap, long long *nblocks);
 /* Whitening in place, like accel_whiten, for callers that cannot allocate
  * device memory.  No counterpart in the reference.  Some hosts forbid
  * cudaMalloc on the data path: a real-time pipeline that sizes all memory at
@@ -252,10 +259,13 @@ int  accel_whiten(accel_ctx *ctx, accel_complex *spec_dev, long long numbins);
  * allocating routine: its scratch is a static 2 MiB device array that every
  * GPU loading the library holds until exit, enough for 131072 whitening
  * blocks (about 1.2e7 bins with the default widths 6/200); larger spectra
- * are rejected with ACCEL_ERR_INVALID.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the array: calls whose GPU
- * work overlaps race, so serialise them (one stream, or synchronise).
+ * are rejected with ACCEL_ERR_INVALID, as are more than 2^31 - 1 bins.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress).  The block table reaches the device by a copy from
+ * host arrays that every call rewrites, so the call must not be made while
+ * its stream is being captured into a CUDA graph: it then returns
+ * ACCEL_ERR_UNSUPPORTED.  All calls share the array: calls whose GPU work
+ * overlaps race, so serialise them (one stream, or synchronise).
  * cuda_stream may be NULL (the legacy default stream). */
 int  accel_whiten_noalloc(accel_complex *spec_dev, long long numbins, int initbuf, int maxbuf,
                           void *cuda_stream);
@@ -357,7 +367,8 @@ int  accel_dedisperse(const float *filterbank_dev, int nchan, long long nsamp, c
 
 /* SIGPROC filterbank reader (host only; the reference reads dedispersed
  * .dat series only, bpd_data.c:9-75, and no function of it is replaced):
- * the header keywords, then nifs = 1 time-major samples of 8 or 16 bits
+ * the header keywords, then nifs = 1 time-major samples of 8 bits (unsigned,
+ * or two's-complement when the one-byte "signed" keyword is nonzero), 16 bits
  * (unsigned) or 32 bits (float).  *data is a malloc'd float32
  * [nchans][nsamples], channel-major as accel_dedisperse takes it (channel c
  * at fch1 + c * foff MHz); free it with accel_free_host. */
@@ -369,6 +380,7 @@ typedef struct accel_filterbank_info {
     double tstart;          /* MJD                                            */
     char source_name[80];
     int header_bytes;
+    int is_signed;          /* "signed" keyword: 8-bit samples are int8      */
 } accel_filterbank_info;
 int  accel_read_filterbank(const char *path, accel_filterbank_info *info, float **data);
 void accel_free_host(void *p);

@@ -63,6 +63,23 @@ def test_roundtrip(tmp_path, nbits):
     assert hdr["source_name"] == "PSR_FAKE"
 
 
+def test_signed_8bit(tmp_path):
+    # the one-byte "signed" keyword marks two's-complement 8-bit samples
+    rng = np.random.default_rng(3)
+    nt, nc = 5000, 16
+    vals = rng.integers(-128, 128, (nt, nc)).astype(np.int8)
+    p = tmp_path / "s8.fil"
+    write_fil(p, vals.view(np.uint8), 8, extra=_s("signed") + b"\x01")
+    hdr, data = read_filterbank(p)
+    assert hdr["is_signed"] == 1
+    assert np.array_equal(data, vals.T.astype(np.float32))
+    # "signed" = 0 keeps unsigned samples
+    write_fil(p, vals.view(np.uint8), 8, extra=_s("signed") + b"\x00")
+    hdr, data = read_filterbank(p)
+    assert hdr["is_signed"] == 0
+    assert np.array_equal(data, vals.view(np.uint8).T.astype(np.float32))
+
+
 def test_nsamples_keyword_limits_and_trailing_bytes_ignored(tmp_path):
     tm = np.arange(40 * 4, dtype=np.float32).reshape(40, 4)
     p = tmp_path / "n.fil"

@@ -4,8 +4,8 @@ ABI, checked by properties that do not need the oracle to run the whole
 trial:
   * every injected signal is the strongest single-harmonic candidate near
     its (r0 + z/2, z);
-  * on the steps that hold the signals, the candidate sets equal the FP64
-    oracle's outside the +-1e-4 band around each cut;
+  * on every step, the candidate sets equal the FP64 oracle's outside the
+    +-1e-4 band around each cut;
   * a trial searched inside a batch of uneven trials gives exactly the
     candidates it gives alone.
 """
@@ -14,6 +14,7 @@ import pytest
 
 from gpu_accelsearch_gb300.synth import synth_series
 from oracle import oracle as O
+from parity_keys import keys, oracle_bounds
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -48,7 +49,10 @@ def test_signals_recovered(big):
         assert abs(best["r"] - (r0 + z / 2)) <= 1.0 and abs(best["z"] - z) <= 4, (best, r0, z)
 
 
-def test_signal_steps_match_oracle(big):
+def test_every_step_matches_oracle(big):
+    # the whole trial (542 overlap-save steps, 0.84 G cells): candidate sets
+    # equal to the FP64 oracle's outside the +-1e-4 band around each cut, on
+    # every step, and the steps holding the signals hold candidates
     s, x = big["s"], big["x"]
     U = s.uselen
     from gpu_accelsearch_gb300.search import first_bin
@@ -59,20 +63,18 @@ def test_signal_steps_match_oracle(big):
     s.search_spectra([d.data_ptr()], [w.size], [rlo])
     gpu = s.candidates()
     cuts = s.power_cuts().astype(np.float64)
+    nsteps = s.step_count(N, DT)
+    assert nsteps == 542
     o = O.Oracle(200, 8, U)
     try:
-        for amp, r0, z in big["sigs"]:
-            step = int((r0 + z / 2 - rlo) // (U // 2))
-            g = gpu[gpu["step"] == step]
-            lo, _, _ = o.run_steps(w, rlo, step, 1, powcut=cuts * (1 - TOL_P))
-            hi, _, _ = o.run_steps(w, rlo, step, 1, powcut=cuts * (1 + TOL_P))
-            gk = {(int(c["step"]), int(round(2 * (c["r"] - (rlo + c["step"] * (U // 2))))),
-                   int(round((c["z"] + 200) / 2)), int(c["numharm"])) for c in g}
-            ok = lambda a: {(int(c["step"]), int(c["ridx"]), int(c["zidx"]), int(c["numharm"])) for c in a}
-            assert len(gk) > 0
-            assert ok(hi) <= gk <= ok(lo), step
+        hi, lo = oracle_bounds(o, w, rlo, 0, nsteps, cuts, tol=TOL_P)
     finally:
         o.close()
+    g = keys(gpu, rlo, U // 2, -200)
+    assert hi <= g <= lo
+    for amp, r0, z in big["sigs"]:
+        step = int((r0 + z / 2 - rlo) // (U // 2))
+        assert any(k[0] == step for k in g), step
 
 
 def test_batch_of_uneven_trials_equals_alone(big):

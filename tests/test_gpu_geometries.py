@@ -1,7 +1,8 @@
 """GPU path against the FP64 oracle at the bench's geometry and its
 neighbours, through the C ABI (the main parity file runs zmax 50, 4
 harmonics, L 2048): zmax 200 with 8 harmonics at L = 4096, 8192 (the bench)
-and 16384, and 16 harmonics at zmax 100.  Between them they run every
+and 16384, 16 harmonics at zmax 100, and the serving banks zmax 300, 100
+and 50 with 8 harmonics at L = 8192.  Between them they run every
 plane-kernel size class (M = 512 .. 8192) and the 8- and 16-harmonic sums.
 
 Tolerances as in test_gpu_parity.py: power planes max |P - P64| /
@@ -18,7 +19,10 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 TOL_P = 1e-4
-GEOMS = [(200, 8, 8192), (200, 8, 4096), (200, 8, 16384), (100, 16, 8192)]
+# the serving banks at the serving segment length: zmax 300, 100 and 50
+# with 8 harmonics at L = 8192
+GEOMS = [(200, 8, 8192), (200, 8, 4096), (200, 8, 16384), (100, 16, 8192),
+         (300, 8, 8192), (100, 8, 8192), (50, 8, 8192)]
 RLO = 16
 SIG_STEP = 10
 

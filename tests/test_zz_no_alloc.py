@@ -34,7 +34,9 @@ def _context_whiten(spec, numbins, init, maxb):
 def test_noalloc_whitening_matches_context_path():
     from gpu_accelsearch_gb300.synth import synth_red_spectrum
     L, whiten = _noalloc()
-    cases = [(1 << 17, 6, 200, 31), (40001, 1000, 1000, 32)]
+    # the warp-per-block kernels (blocks of at most 1024 bins) and the
+    # CTA-per-block kernels with opt-in shared memory (blocks of 4096 bins)
+    cases = [(1 << 17, 6, 200, 31), (40001, 1000, 1000, 32), (1 << 20, 600, 4096, 33)]
     for numbins, init, maxb, seed in cases:
         spec = synth_red_spectrum(numbins + 1, seed=seed)
         want = _context_whiten(spec, numbins, init, maxb)
@@ -54,3 +56,21 @@ def test_noalloc_rejects_oversize():
     rc = whiten(d.data_ptr(), 1 << 30, 6, 200, None)
     assert rc == -1
     assert "static scratch" in L.accel_last_error().decode()
+
+
+def test_noalloc_refused_inside_stream_capture():
+    # the block table is copied from host arrays that the next call
+    # rewrites, so a captured call is refused and nothing is enqueued
+    L, whiten = _noalloc()
+    d = torch.zeros(2 * 4096, dtype=torch.float32, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side):
+            d.add_(1.0)
+            rc = whiten(d.data_ptr(), 4000, 6, 200, torch.cuda.current_stream().cuda_stream)
+    assert rc == -5
+    assert "capture" in L.accel_last_error().decode()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(d[0]) == 1.0
