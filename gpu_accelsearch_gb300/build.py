@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "bank.cu", "search.cu", "search_plane_lo.cu", "search_plane_hi.cu",
            "search_fund_lo.cu", "search_fund_hi.cu", "tune.cu", "whiten.cu", "compat.cu",
            "server.cu", "sift.cu", "optimize.cu", "dedisperse.cu",
-           "filterbank.cu"]
+           "filterbank.cu", "compat_cxx.cu"]
 EXTRA = {"bank.cu": ["-fmad=false"], "compat.cu": ["-Xcompiler", "-ffp-contract=off"],
          "dedisperse.cu": ["-Xcompiler", "-ffp-contract=off"]}
 HEADERS = ["accel_common.cuh", "accel_internal.h", "context.h", "fft_smem.cuh", "search_kernels.cuh"]
@@ -54,7 +54,7 @@ def _stale(target: str, deps) -> bool:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, src.replace(".cu", ".o"))
     deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + \
-        [os.path.join(ROOT, "include", h) for h in ("accelsearch.h", "bpd_compat.h")] + [__file__]
+        [os.path.join(ROOT, "include", h) for h in ("accelsearch.h", "bpd_compat.h", "bpd_compat_cxx.h")] + [__file__]
     if not _stale(obj, deps):
         return obj
     cmd = [nvcc()] + _flags() + EXTRA.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]

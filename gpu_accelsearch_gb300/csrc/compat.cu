@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -759,6 +760,47 @@ void addPowers(int fundamental_numzs, int fundamental_numrs, int subharm_fftlen,
                                       subharm_zlo, subharm_rlo, p, q, reinterpret_cast<const float2*>(data), scale,
                                       output_powers, (long long)fullrlo);
     if (cudaGetLastError() != cudaSuccess) fail(ACCEL_ERR_CUDA, "addPowers");
+}
+
+// ------------------------------------------ bpd_math.h, app_utilities.h
+float fast_median(float arr[], int n) {
+    if (!arr || n <= 0) return 0.f;
+    // the order statistic of rank (n - 1) / 2, input reordered around it
+    std::nth_element(arr, arr + (n - 1) / 2, arr + n);
+    return arr[(n - 1) / 2];
+}
+
+float inverse_square_root(float x) { return rsqrt_magic_host(x); }
+
+int fast_log2(int n) {
+    int x = 0;
+    for (; n > 1; n >>= 1) x++;
+    return x;
+}
+
+int toNearestInt(double x) { return nearest_int(x); }
+
+long long get2PowerNGreaterThan(long long x) {
+    long long p = 1;
+    while (p < x && p < (1LL << 62)) p <<= 1;
+    return p;
+}
+
+void logMessage(const char* message, ...) {
+    va_list ap;
+    va_start(ap, message);
+    vprintf(message, ap);
+    va_end(ap);
+    printf("\n");
+}
+
+void throwError(const char* errorMessage, ...) {
+    va_list ap;
+    va_start(ap, errorMessage);
+    vprintf(errorMessage, ap);
+    va_end(ap);
+    printf("\n");
+    exit(EXIT_FAILURE);
 }
 
 }  // extern "C"

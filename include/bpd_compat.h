@@ -4,9 +4,11 @@
  * libaccelsearch.so on its own GB300 kernels.  A caller of the reference's
  * headers/bpd_search.cuh, bpd_subharmonics.cuh, bpd_fft.cuh, bpd_noise.h and
  * bpd_candidates.cuh includes this header instead and links
- * -laccelsearch.  Everything here has C linkage (the reference's .cu
- * functions have C++ linkage; a C++ caller includes this header and gets the
- * same names).
+ * -laccelsearch.  Everything here has C linkage.  The reference's .cu
+ * functions have C++ linkage: the same functions with that linkage (the
+ * symbols an object compiled against the reference's own headers needs) are
+ * declared in bpd_compat_cxx.h and exported too, so such an object links
+ * against libaccelsearch.so unchanged.
  *
  * Differences kept on purpose: errors do not exit the process -- the
  * functions are void as in the reference, so check accel_compat_status()
@@ -23,6 +25,9 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* The structs below are shared with include/bpd_compat_cxx.h, which defines
+ * BPD_COMPAT_TYPES_ONLY to take them without the C-linkage functions. */
 
 /* headers/bpd_subharmonics.cuh:13-25 */
 typedef struct SubharmonicInfo {
@@ -64,6 +69,8 @@ typedef struct Candidates {
     double *hizs;
     rderivs *derivs;
 } Candidates;
+
+#ifndef BPD_COMPAT_TYPES_ONLY
 
 /* Runtime replacement of the reference's ACCEL_USELEN (bpd_common.h:24),
  * default 32000; it must be even and below 65536. */
@@ -157,6 +164,27 @@ Candidates *search_ffdot_powers_n(ffdotInfo *ffdot, int numharm, float powcut,
  * `cands` argument is ignored (the reference returns it unchanged). */
 Candidates *search_ffdot_powers(ffdotInfo *ffdot, int numharm, float powcut, long long numindep,
                                 Candidates *cands);
+
+/* bpd_math.h:17-25 -- the reference's host helpers (C linkage, as its
+ * driver includes bpd_math.h inside extern "C"): fast_median returns the
+ * element of rank (n-1)/2 (the lower median) and reorders arr, like the
+ * reference's quickselect; inverse_square_root is the magic-constant
+ * 0x5f3759df estimate with one Newton step, rounded operation by operation;
+ * fast_log2 is floor(log2(n)) for n >= 1; toNearestInt rounds half away from
+ * zero; get2PowerNGreaterThan is the first power of two >= x. */
+float     fast_median(float arr[], int n);
+float     inverse_square_root(float x);
+int       fast_log2(int n);
+int       toNearestInt(double x);
+long long get2PowerNGreaterThan(long long x);
+
+/* app_utilities.h:12-13 -- printf-style logging with a newline; throwError
+ * prints and exits the process, as the reference's does (it is the caller's
+ * own error path; nothing in this library calls it). */
+void logMessage(const char *message, ...);
+void throwError(const char *errorMessage, ...);
+
+#endif /* BPD_COMPAT_TYPES_ONLY */
 
 #ifdef __cplusplus
 }

@@ -21,26 +21,49 @@ def lib():
     return N.lib()
 
 
-def declared_functions():
+def declared_functions(headers=None):
     names = []
     for hdr in sorted(os.listdir(os.path.join(ROOT, "include"))):
-        if not hdr.endswith(".h"):
+        if not hdr.endswith(".h") or (headers and hdr not in headers):
             continue
         text = open(os.path.join(ROOT, "include", hdr)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"^#.*$", "", text, flags=re.M)
         for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", text, flags=re.M):
             if m.group(1) not in ("if", "defined"):
                 names.append(m.group(1))
     return sorted(set(names))
 
 
+def exported_cxx(lib_path):
+    """Demangled names of the library's exported C++-linkage functions."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("no nm")
+    out = subprocess.run([nm, "-D", "--defined-only", "-C", lib_path], check=True, capture_output=True,
+                         text=True).stdout
+    return {line.split(" ", 2)[2].split("(")[0] for line in out.splitlines()
+            if len(line.split(" ", 2)) == 3 and "(" in line}
+
+
 def test_exports_every_declared_function(lib):
-    names = declared_functions()
+    # C linkage (accelsearch.h, bpd_compat.h): visible to ctypes by name
+    names = declared_functions(("accelsearch.h", "bpd_compat.h"))
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     # and the Python binding covers the header
     assert set(N.exported_symbols()) <= set(names)
+    # C++ linkage (bpd_compat_cxx.h): exported under the mangled names (the
+    # link tests in test_cxx_linkage_cpu.py check the exact signatures); its
+    # extern "C" block names C-linkage functions checked above
+    cxx = declared_functions(("bpd_compat_cxx.h",))
+    have = exported_cxx(N.LIB_PATH)
+    missing = [n for n in cxx if n not in have and not hasattr(lib, n)]
+    assert not missing, missing
+    assert {"createSubharmonicInfo", "perform_harmonic_summing", "spreadData", "__checkCudaErrors"} <= have
 
 
 def test_config_defaults(lib):
