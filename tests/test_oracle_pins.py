@@ -141,3 +141,25 @@ def test_exact_rsqrt_mode_switch():
     w_magic = O.deredden(spec)
     assert not np.array_equal(w_exact, w_magic)
     assert np.abs(np.abs(w_exact) / np.abs(w_magic) - 1)[1:].max() < 2e-3
+
+
+def test_oracle_planes_equal_reference_kernels():
+    # the oracle's FP64 restatement of convolveSignal / inverse FFT /
+    # generatePowers / addPowers against the reference's own kernel source
+    # run on the host (tests/golden/reference_planes.npz): fundamental powers
+    # and every harmonic stage sum of one step, over the stored columns
+    import golden_planes as GP
+    g = GP.load()
+    for case, step, zmax, numharm, uselen, numbins, startr, (c0, c1), ref in GP.cases(g):
+        w = GP.spectrum(g, case, step, numbins)
+        orc = O.Oracle(zmax, numharm, uselen)
+        try:
+            rlo = int(g[case + "_meta"][5])
+            k = (startr - rlo) // (uselen // 2)
+            _, planes, _ = orc.run_steps(w, rlo, k, 1, want_planes=True)
+        finally:
+            orc.close()
+        got = planes[0][:, :, c0:c1]
+        assert got.shape == ref.shape, (case, step)
+        err = (np.abs(got - ref) / np.maximum(ref, 1.0)).max()
+        assert err < 2e-6, (case, step, err)
