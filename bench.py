@@ -337,33 +337,50 @@ def precision_report(seeds: int, device: int):
 
 
 # ------------------------------------------------------------ cpu baseline
-def cpu_baseline(seconds: float):
-    """The oracle (FP64 restatement of the reference path) on a bounded
-    sample: overlap-save steps of one 2^22-sample trial, all host threads."""
-    from gpu_accelsearch_gb300.synth import synth_series
-    from oracle import oracle as O
-    n = 1 << 22
-    x = synth_series(n, seed=1, signals=[(0.05, 200000.25, 40.0)])
-    spec = np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2]
-    w = O.deredden(spec)
-    U = 7734
-    orc = O.Oracle(ZMAX, NUMHARM, U)
-    cores = os.cpu_count() or 1
-    cuts = np.array([O.power_cut(6.0, 1 << s) for s in range(orc.nstages)])
-    rlo = int(np.floor(np.float32(n) * np.float32(DT)))
-    t = time.perf_counter()
-    orc.run_steps(w, rlo, 0, 1, powcut=cuts, cap=1 << 16, nthreads=cores)
-    t1 = time.perf_counter() - t
-    nsteps = int(max(1, min(541, seconds / max(t1, 1e-3))))
-    t = time.perf_counter()
-    orc.run_steps(w, rlo, 1, nsteps, powcut=cuts, cap=1 << 16, nthreads=cores)
-    el = time.perf_counter() - t
-    cells = nsteps * U * int(orc.geom[0, 3])
-    orc.close()
-    return {"value": cells / el, "unit": "cells/s", "cores": cores, "kind": "port", "seconds": el,
-            "sample": f"{nsteps} overlap-save steps of one 2^22-sample trial (zmax=200, 8 "
-                      f"harmonics, L=8192, uselen=7734): FP64 oracle planes + harmonic sum + "
-                      f"threshold, {el:.1f} s"}
+class CpuBaseline:
+    """The CPU baseline: the FP32 restatement of the reference pipeline
+    (oracle/cpu_fp32.py: the reference's host segment preparation, single-
+    precision FFTs, its convolution / power / harmonic-sum arithmetic) over
+    overlap-save steps of one 2^22-sample trial of the batched workload's
+    geometry (zmax 200, 8 harmonics, L 8192), one step per task on a spawn
+    process pool with one process per host core."""
+
+    def __init__(self):
+        from gpu_accelsearch_gb300.synth import synth_series
+        from oracle import cpu_fp32 as F
+        from oracle import oracle as O
+        n = 1 << 22
+        x = synth_series(n, seed=1, signals=[(0.05, 200000.25, 40.0)])
+        spec = np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2]
+        self.w = O.deredden(spec)
+        self.U = 7734
+        self.numzs0 = int(O.bank_geometry(ZMAX, NUMHARM, self.U)[0, 3])
+        self.cuts = np.array([O.power_cut(6.0, 1 << s) for s in range(4)])
+        self.rlo = int(np.floor(np.float32(n) * np.float32(DT)))
+        self.nsteps_max = O.step_count(n // 2, self.rlo, self.U)
+        self.pool = F.StepPool(ZMAX, NUMHARM, self.U, self.w)
+        self.cores = self.pool.processes
+        self.per_step = None
+
+    def sample(self, seconds: float):
+        if self.per_step is None:  # calibrate on one step per process
+            el, _ = self.pool.run([self.rlo + k * (self.U // 2) for k in range(self.cores)], self.cuts)
+            self.per_step = el / self.cores
+        nsteps = int(max(self.cores, min(self.nsteps_max, seconds / max(self.per_step, 1e-4))))
+        startrs = [self.rlo + k * (self.U // 2) for k in range(nsteps)]
+        el, nc = self.pool.run(startrs, self.cuts)
+        cells = nsteps * self.U * self.numzs0
+        return {"value": cells / el, "unit": "cells/s", "cores": self.cores, "kind": "port",
+                "seconds": el, "candidates": nc,
+                "implementation": "FP32 restatement of the reference pipeline (oracle/cpu_fp32.py): "
+                                  "reference host segment preparation, scipy.fft single-precision "
+                                  "FFTs, convolveSignal/generatePowers/addPowers arithmetic, "
+                                  "one step per process",
+                "sample": f"{nsteps} overlap-save steps of one 2^22-sample trial (zmax=200, 8 "
+                          f"harmonics, L=8192, uselen=7734), {self.cores} processes, {el:.1f} s"}
+
+    def close(self):
+        self.pool.close()
 
 
 def run_reference(args):
@@ -371,24 +388,27 @@ def run_reference(args):
     if rank != 0:
         return
     per = max(1.0, args.cpu_seconds / 3)
-    for _ in range(args.warmup):
-        cpu_baseline(per / 4)
-    runs = [cpu_baseline(per) for _ in range(max(1, args.steps))]
+    cpu = CpuBaseline()
+    try:
+        for _ in range(args.warmup):
+            cpu.sample(per / 4)
+        runs = [cpu.sample(per) for _ in range(max(1, args.steps))]
+    finally:
+        cpu.close()
     v = float(np.median([r["value"] for r in runs]))
     cb = dict(runs[-1])
     cb["value"] = v
-    # one step = one bounded sample of the workload (the sample is in cpu_baseline)
+    # one step = one bounded sample of the workload (the sample is in cb)
     ms = 1e3 * float(np.median([r["seconds"] for r in runs]))
     line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded N(0,1) float32 series with an injected sinusoid",
             "impl": "reference",
             "config": {"workload": "bounded sample of the batched configuration on the host: "
                                    "overlap-save steps of one 2^22-sample trial, zmax=200, "
                                    "8 harmonics, L=8192",
-                       "implementation": "CPU oracle port of the reference pipeline "
-                                         "(oracle/accel_oracle.c), OpenMP over templates"},
+                       "implementation": cb["implementation"]},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -403,6 +423,31 @@ def load_peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def measure_fp32_peak(torch) -> float:
+    """FP32 CUDA-core throughput of this GPU in TFLOP/s: cuBLAS FP32 GEMM
+    of 8192^3 with TF32 off, best of 5 after 2 warm-ups (CUDA events)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(2):
+            c = a @ b
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            c = a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        del a, b, c
+        return 2.0 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
 
 
 def load_traffic(kernel: str):
@@ -543,14 +588,25 @@ def run_ours(args):
         plain = {"value": pv, "unit": "cells/s",
                  "workload": "one 2^22-sample trial, one overlap-save step per launch group "
                              f"({pn} steps, L={FFTLEN}): the reference's step-at-a-time control flow"}
+        # the batch itself, one trial per search call (device-resident
+        # series, the batched search's tuned launch shape)
         q = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local)
         q.set_tuning(chunk_segments=chunk, plane_split=split, **extra)
-        qn, qv = time_trial(q)
+        for i in range(min(4, len(ptrs))):
+            q.search([ptrs[i]], DT, on_device=True, nsamples=[lengths[i]])
+        torch.cuda.synchronize()
+        q.reset_stats()
+        t3 = time.perf_counter()
+        for i in range(len(ptrs)):
+            q.search([ptrs[i]], DT, on_device=True, nsamples=[lengths[i]])
+        torch.cuda.synchronize()
+        wall3 = time.perf_counter() - t3
+        dev3 = q.stats()["search_ms"] / 1e3
         q.close()
-        plain_trial = {"value": qv, "unit": "cells/s",
-                       "workload": f"one 2^22-sample trial per search ({qn} steps), launch groups of "
-                                   f"{chunk} segments, L={fftlen}: the batched search's own launch "
-                                   "shape on a single trial"}
+        plain_trial = {"value": cells / dev3, "unit": "cells/s", "wall_value": cells / wall3,
+                       "workload": f"the same {len(ptrs)} trials, one accel_search call per trial "
+                                   f"(launch groups of {chunk} segments, L={fftlen}): what searching "
+                                   "the trials together adds"}
 
     if rank != 0:
         s.close()
@@ -583,34 +639,35 @@ def run_ours(args):
              "fund": "k_fund_sum (fundamental plane fused with harmonic sum + threshold)"}
     tr = load_traffic(dom) if dom else None
     roofline = None
+    import math
+    # algorithmic FP32 work of one segment's plane rows: two M-point inverse
+    # FFTs per template at the radix-2 count 5 M log2 M, plus the template
+    # products (6 flops per point) and the powers (3 flops per point)
+    flops_seg = sum(h.numzs * (2 * 5 * (h.fftlen // 2) * math.log2(h.fftlen // 2) + 18 * (h.fftlen // 2))
+                    for h in s.harmonics)
+    fp32_peak = measure_fp32_peak(torch)
     if dom:
         pk = per_kernel[dom]
-        roofline = {"bound": "hbm", "kernel": names[dom], "achieved": pk["achieved"], "peak": peak,
-                    "unit": "GB/s", "frac": pk["achieved"] / peak, "peak_source": peak_kind,
-                    "algorithmic_bytes_per_launch": pk["bytes_per_launch"],
-                    "traffic": (tr * segs / max(pk["launches"], 1)) if tr else None,
-                    "note": "achieved = algorithmic bytes (4 B per plane cell moved) per launch / "
-                            "mean CUDA-event time of its launches in the timed region",
-                    "per_kernel": {n: {"achieved_GBs": round(v["achieved"], 1),
-                                       "frac": round(v["achieved"] / peak, 4)}
-                                   for n, v in per_kernel.items()}}
-    # the compute side of the plane kernel: algorithmic FP32 work of every
-    # row (two M-point inverse FFTs at 5 M log2 M flops each, the complex
-    # template products and the powers) over the same CUDA-event time,
-    # against the nominal FP32 rate (SMs x 128 lanes x 2 flops x max clock;
-    # no measured FP32 peak exists for this machine)
-    if roofline is not None and "plane" in per_kernel and not fused:
-        import math
-        flops_seg = sum(h.numzs * (2 * 5 * (h.fftlen // 2) * math.log2(h.fftlen // 2) + 18 * (h.fftlen // 2))
-                        for h in s.harmonics)
-        props = torch.cuda.get_device_properties(local)
-        mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
-        fp32_peak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
-        achieved_tf = flops_seg * segs / (k["plane"]["ms"] / 1e3) / 1e12
-        roofline["fp32_side"] = {"kernel": "k_plane", "flops_per_segment": flops_seg,
-                                 "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                                 "frac": achieved_tf / fp32_peak,
-                                 "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock"}
+        hbm_axis = {"achieved": pk["achieved"], "peak": peak, "unit": "GB/s", "frac": pk["achieved"] / peak,
+                    "peak_source": peak_kind, "algorithmic_bytes_per_launch": pk["bytes_per_launch"],
+                    "note": "algorithmic bytes (4 B per plane cell moved) per launch / mean CUDA-event "
+                            "time of its launches in the timed region"}
+        traffic = (tr * segs / max(pk["launches"], 1)) if tr else None
+        if dom in ("plane", "fund"):
+            # what bounds the plane kernel (ncu: issue slots 68 %, FP32 pipe
+            # 52 %, L1/shared 69 %, DRAM 19 %) is its FP32 work, not HBM
+            achieved_tf = flops_seg * segs / (k[dom]["ms"] / 1e3) / 1e12
+            roofline = {"bound": "fp32", "kernel": names[dom], "achieved": achieved_tf,
+                        "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
+                        "peak_source": "measured in this run: cuBLAS FP32 GEMM 8192^3 with TF32 off "
+                                       "(no FP32 figure in MEASURED_PEAKS.json)",
+                        "flops_per_segment": flops_seg, "traffic": traffic, "hbm": hbm_axis,
+                        "note": "achieved = algorithmic FP32 flops per launch (radix-2 FFT count) / "
+                                "mean CUDA-event time of its launches in the timed region"}
+        else:
+            roofline = dict(hbm_axis, bound="hbm", kernel=names[dom], traffic=traffic)
+        roofline["per_kernel"] = {n: {"achieved_GBs": round(v["achieved"], 1), "frac_hbm": round(v["achieved"] / peak, 4)}
+                                  for n, v in per_kernel.items()}
     step_roofline = {"bytes_per_cell": bytes_per_cell,
                      "achieved": value / world * bytes_per_cell / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": value / world * bytes_per_cell / 1e9 / peak,
@@ -618,7 +675,13 @@ def run_ours(args):
     tot_ms = max(sum(x["ms"] for x in k.values()), 1e-9)
     kern = {name: {"launches": v["launches"], "ms": round(v["ms"], 3),
                    "share": round(v["ms"] / tot_ms, 4)} for name, v in k.items() if v["launches"]}
-    cb = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    cb = None
+    if args.cpu_seconds > 0:
+        cpu = CpuBaseline()
+        try:
+            cb = cpu.sample(args.cpu_seconds)
+        finally:
+            cpu.close()
     dedisp = run_dedisperse(local) if args.serving_seconds > 0 else None
     serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
     # the same stream at half the rate: latency when the GPU is not saturated
