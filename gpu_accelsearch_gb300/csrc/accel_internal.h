@@ -184,6 +184,33 @@ constexpr int kHsumTileFloats = 15360;
 constexpr int kPipeBuffers = 4;   // tile buffers of the pipelined harmonic sum
 constexpr int kPipeSmemMax = 222 * 1024;  // their dynamic shared memory (227 KB less the static tables)
 
+// A launch group's plane rows and harmonic-sum tiles in one persistent
+// launch (k_step, step_kernel.cuh).
+constexpr int kStepClasses = 4;
+constexpr int kStepLag = 1;  // tiles of segment j run beside the rows of segment j + kStepLag
+
+struct StepArgs {
+    HsumArgs hs;                            // bank-order harmonics, planes, cuts, candidates, error word
+    const float2* dbuf;                     // segment spectra [nseg][dstride]
+    long long dstride;
+    float* planes;                          // == hs.planes, written by the plane items
+    int ncls;                               // plane classes (segment lengths M), largest first
+    int cls_M[kStepClasses];
+    int cls_nh[kStepClasses];
+    int cls_h[kStepClasses][kMaxHarm];      // bank index of each harmonic of the class
+    int cls_zbase[kStepClasses][kMaxHarm];  // its first row within the class
+    int cls_ntpl[kStepClasses];             // rows of the class
+    int cls_item0[kStepClasses + 1];        // first plane item of each class within a segment
+    int P, T;                               // plane items and sum tiles per segment
+    int rows;                               // plane rows per segment
+    int nti;                                // tiles across the columns
+    int nseg, lag;                          // lag <= nseg
+    long long nitems;
+    unsigned* next;                         // work counter, zero at launch
+    unsigned* done;                         // [nseg] plane rows finished, zero at launch
+};
+int launch_step(const StepArgs& a, int mmax, int use_fp16, const float2* tw, cudaStream_t st);
+
 // Record an error message for accel_last_error() and return `code`.
 int set_error(int code, const char* fmt, ...);
 

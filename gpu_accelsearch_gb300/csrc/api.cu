@@ -107,7 +107,7 @@ int ensure_device(accel_ctx* c) {
     return ACCEL_OK;
 }
 
-enum { K_PREP = 0, K_PLANE = 1, K_HSUM = 2, K_WHITEN = 3, K_RFFT = 4, K_FUND = 5 };
+enum { K_PREP = 0, K_PLANE = 1, K_HSUM = 2, K_WHITEN = 3, K_RFFT = 4, K_FUND = 5, K_STEP = 6 };
 
 cudaEvent_t take_event(accel_ctx* c) {
     cudaEvent_t e = nullptr;
@@ -343,6 +343,7 @@ int alloc_work(accel_ctx* c) {
         CK(cudaEventCreateWithFlags(&c->ev_plane[b], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&c->ev_sum[b], cudaEventDisableTiming));
     }
+    CK(cudaMalloc(&c->d_step, sizeof(unsigned) * ((size_t)chunk + 1)));
     c->cand_cap = c->cfg.cand_capacity > 0 ? c->cfg.cand_capacity : (1LL << 22);
     CK(cudaMalloc(&c->d_cands, sizeof(RawCand) * c->cand_cap));
     // [0] candidate count, [1] kernel error bits
@@ -567,6 +568,94 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
     return ACCEL_OK;
 }
 
+// Whether the persistent plane-and-sum kernel can take this plan: the
+// tiled sum applies, the largest segment length is 8192 (256 threads, one
+// per tile column), and every class is one of 4096, 2048, 1024, 512 points
+// (at most four classes).
+bool step_plan_ok(const accel_ctx* c) {
+    if (!c->tile_ok || !c->hsum_tiled || c->fused_sum || !c->d_step) return false;
+    if (c->mvals.empty() || c->mvals.size() > (size_t)kStepClasses) return false;
+    int mmax = 0;
+    for (int M : c->mvals) {
+        if (M != 4096 && M != 2048 && M != 1024 && M != 512) return false;
+        mmax = std::max(mmax, M);
+    }
+    return mmax == 4096;
+}
+
+// One launch group as a single persistent launch: plane rows and harmonic-
+// sum tiles of its segments from one work queue (k_step).  The segments'
+// spectra must have been prepared (k_prep) on the same stream before.
+int run_step(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base) {
+    StepArgs sa{};
+    HsumArgs& ha = sa.hs;
+    for (int h = 0; h < c->nh; h++) {
+        ha.h[h] = c->hp[h];
+        ha.stage_of[h] = c->stage_of[h];
+    }
+    ha.nh = c->nh;
+    ha.uselen = c->uselen;
+    ha.numzs0 = c->numzs0;
+    ha.zlo0 = c->zlo0;
+    for (int s = 0; s < c->nstages; s++) ha.cut[s] = c->cuts[s];
+    ha.segs = d_segs;
+    ha.planes = c->planes;
+    ha.pstride = c->pstride;
+    ha.cands = c->d_cands;
+    ha.ncand = c->d_ncand;
+    ha.cap = c->cand_cap;
+    ha.seg_base = seg_base;
+    ha.stage_out = nullptr;
+    ha.nstages = c->nstages;
+    ha.err = c->d_ncand + 1;
+    ha.tile_floats = c->tile_floats;
+    ha.test_extra_tx = c->wait_test ? 16u : 0u;
+    sa.dbuf = c->dbuf;
+    sa.dstride = c->dstride;
+    sa.planes = c->planes;
+    int mmax = 0;
+    for (int M : c->mvals) mmax = std::max(mmax, M);
+    // classes largest first, harmonics of a class in bank order
+    std::vector<int> ms(c->mvals);
+    std::sort(ms.begin(), ms.end(), std::greater<int>());
+    sa.ncls = (int)ms.size();
+    int items = 0, rows = 0;
+    for (int k = 0; k < sa.ncls; k++) {
+        sa.cls_M[k] = ms[k];
+        int n = 0, zb = 0;
+        for (int h = 0; h < c->nh; h++) {
+            if (c->hp[h].M != ms[k]) continue;
+            sa.cls_h[k][n] = h;
+            sa.cls_zbase[k][n] = zb;
+            zb += c->hp[h].numzs;
+            n++;
+        }
+        sa.cls_nh[k] = n;
+        sa.cls_ntpl[k] = zb;
+        sa.cls_item0[k] = items;
+        const int per = mmax / ms[k];
+        items += (zb + per - 1) / per;
+        rows += zb;
+    }
+    sa.cls_item0[sa.ncls] = items;
+    sa.P = items;
+    sa.nti = (c->uselen + kHsumTileI - 1) / kHsumTileI;
+    sa.T = sa.nti * ((c->numzs0 + kHsumTileZ - 1) / kHsumTileZ);
+    sa.rows = rows;
+    sa.nseg = nseg;
+    sa.lag = std::min(kStepLag, nseg);
+    sa.nitems = (long long)(sa.P + sa.T) * nseg;
+    if (sa.nitems >= (1LL << 31)) return set_err(ACCEL_ERR_UNSUPPORTED, "launch group of %d segments too large", nseg);
+    sa.next = c->d_step;
+    sa.done = c->d_step + 1;
+    CK(cudaMemsetAsync(c->d_step, 0, sizeof(unsigned) * (size_t)(nseg + 1), c->stream));
+    ProfScope ps(c, K_STEP, 1);
+    c->stats.segments += nseg;
+    c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
+    CKL(launch_step(sa, mmax, c->cfg.template_fp16, c->tw, c->stream), "persistent plane and sum");
+    return ACCEL_OK;
+}
+
 // Record the launches that issue() makes into a CUDA graph and launch it on
 // the context's stream.  issue() runs against two non-blocking capture
 // streams standing in for stream and stream2, so that nothing else ordered
@@ -661,7 +750,8 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         if (total > 0)
             CK(cudaMemcpyAsync(c->d_segs, c->h_segs, sizeof(SegDesc) * total, cudaMemcpyHostToDevice,
                                c->stream));
-        const bool overlap = c->overlap && !c->fused_sum && c->planes2 && c->stream2;
+        const bool persistent = c->persistent && step_plan_ok(c);
+        const bool overlap = !persistent && c->overlap && !c->fused_sum && c->planes2 && c->stream2;
         if (overlap) {
             // fork: stream2 starts after everything queued so far on the main stream
             CK(cudaEventRecord(c->ev_fork, c->stream));
@@ -679,6 +769,12 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
             int n = (int)std::min<long long>(c->chunk, total - g);
             rc = prepare_upto(c->h_segs[g + n - 1].trial);
             if (rc) return rc;
+            if (persistent) {
+                rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, false, false, false);
+                if (!rc) rc = run_step(c, c->d_segs + g, n, (int)g);
+                if (rc) return rc;
+                continue;
+            }
             if (!overlap) {
                 rc = run_group(c, c->d_segs + g, n, (int)g, nullptr, nullptr, nullptr, true, true, true,
                                c->fused_sum != 0);
@@ -713,7 +809,9 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (c->h_ncand[1])
-        return set_err(ACCEL_ERR_CUDA, "harmonic sum: a tile's copy wait timed out (error bits %llx)",
+        return set_err(ACCEL_ERR_CUDA,
+                       "harmonic sum: a bounded wait timed out (error bits %llx: 1 a tile's copies, 2 a "
+                       "segment's plane rows)",
                        c->h_ncand[1]);
     unsigned long long nraw = *c->h_ncand;
     c->last_raw = nraw;
@@ -783,6 +881,7 @@ void free_ctx(accel_ctx* c) {
     cudaFree(c->dbuf);
     cudaFree(c->planes);
     cudaFree(c->planes2);
+    cudaFree(c->d_step);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->gcap) cudaStreamDestroy(c->gcap);
     if (c->gcap2) cudaStreamDestroy(c->gcap2);
@@ -949,6 +1048,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->serial_sum = !c->overlap;
     t->hsum_pipelined = c->hsum_pipe;
     t->graph = c->use_graph;
+    t->persistent = c->persistent;
     t->wait_test = c->wait_test;
     return ACCEL_OK;
 }
@@ -965,6 +1065,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->overlap = t->serial_sum == 0;
     c->hsum_pipe = t->hsum_pipelined != 0;
     c->use_graph = t->graph != 0;
+    c->persistent = t->persistent != 0;
     c->wait_test = t->wait_test != 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));
@@ -972,13 +1073,16 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
         cudaFree(c->dbuf);
         cudaFree(c->planes);
         cudaFree(c->planes2);
+        cudaFree(c->d_step);
         c->dbuf = nullptr;
         c->planes = nullptr;
         c->planes2 = nullptr;
+        c->d_step = nullptr;
         c->chunk = t->chunk_segments;
         CK(cudaMalloc(&c->dbuf, sizeof(float2) * c->dstride * c->chunk));
         CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * c->chunk));
         CK(cudaMalloc(&c->planes2, sizeof(float) * c->pstride * c->chunk));
+        CK(cudaMalloc(&c->d_step, sizeof(unsigned) * ((size_t)c->chunk + 1)));
     }
     return ACCEL_OK;
 }

@@ -69,6 +69,8 @@ struct accel_ctx {
     bool tile_ok = false;     // the tiled harmonic sum fits its shared buffer
     int hsum_tiled = 1;
     int hsum_pipe = 0;      // persistent pipelined tile kernel
+    int persistent = 0;     // plane rows and sum tiles of a group in one launch (k_step)
+    unsigned* d_step = nullptr;  // k_step's work counter and per-segment row counts
     int wait_test = 0;      // failure-detection test: every tile's copy wait runs out
     // CUDA graph of a device-resident search: recorded on two non-blocking
     // capture streams standing in for stream/stream2, launched on stream

@@ -19,6 +19,19 @@
 namespace accel {
 
 __device__ __forceinline__ int fft_pad(int i) { return i + (i >> 4); }
+
+// Barrier between passes: the whole CTA (the default), or a named barrier
+// over the group of threads doing one transform (several transforms of a
+// smaller size side by side in one CTA, each group on its own barrier).
+struct CtaSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupSync {
+    int id, nthreads;  // barrier 1..15, a multiple of 32 threads
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+    }
+};
 template <int M> struct FftShape {
     static constexpr int T = M / 16;
     static constexpr int PADDED = M + M / 16;
@@ -206,10 +219,10 @@ __device__ __forceinline__ void apply_tw16(float2 (&v)[NB][16], const Tw16& p) {
 // One Stockham pass of radix R over NB transforms.  FIRST: input already in
 // registers (time order).  LAST: output left in registers (frequency order).
 // PRE: twiddles of a radix-16 pass supplied by the caller (Q == 1).
-template <int M, int R, int NS, bool FIRST, bool LAST, int DIR, int NB>
+template <int M, int R, int NS, bool FIRST, bool LAST, int DIR, int NB, class Sync = CtaSync>
 __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
                                          const float2* __restrict__ tw, int t,
-                                         const Tw16* pre = nullptr) {
+                                         const Tw16* pre = nullptr, Sync sync = Sync()) {
     constexpr int T = M / 16;
     constexpr int Q = 16 / R;
     constexpr int PM = FftShape<M>::PADDED;
@@ -234,7 +247,7 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
                     for (int r = 0; r < R; r++)
                         a[nb][q + r * Q] = sm[nb * PM + fft_pad(t + q * T + r * (M / R))];
         }
-        __syncthreads();
+        sync();
     }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -278,7 +291,7 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
             }
         }
     }
-    if constexpr (!LAST) __syncthreads();
+    if constexpr (!LAST) sync();
 }
 
 // Full transform: radix-16 passes, the leftover factor (2, 4 or 8) last.
@@ -288,35 +301,35 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
 // of an index side by side.  The twiddles of the radix-16 passes after the
 // first are loaded up front.  Shared memory may be rewritten as soon as
 // this returns.
-template <int M, int DIR, int NB>
+template <int M, int DIR, int NB, class Sync = CtaSync>
 __device__ __forceinline__ void fft_run(float2 (&a)[NB][16], float2* sm, const float2* __restrict__ tw,
-                                        int t) {
+                                        int t, Sync sync = Sync()) {
     static_assert(M >= kMinM && M <= kMaxM && (M & (M - 1)) == 0, "M must be a power of two");
     if constexpr (M == 64) {
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 4, 16, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 4, 16, false, true, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
     } else if constexpr (M == 128) {
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 8, 16, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 8, 16, false, true, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
     } else if constexpr (M == 256) {
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 16, false, true, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
     } else if constexpr (M == 512 || M == 1024 || M == 2048) {
         constexpr int RL = M / 256;
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, RL, 256, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 16, false, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, RL, 256, false, true, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
     } else if constexpr (M == 4096) {
         const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 256, false, true, DIR, NB>(a, sm, tw, t, &p2);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 16, false, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 256, false, true, DIR, NB, Sync>(a, sm, tw, t, &p2, sync);
     } else {  // 8192
         const Tw16 p2 = load_tw16<DIR>(tw, t & 255, 4096);
-        fft_pass<M, 16, 1, true, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 16, false, false, DIR, NB>(a, sm, tw, t);
-        fft_pass<M, 16, 256, false, false, DIR, NB>(a, sm, tw, t, &p2);
-        fft_pass<M, 2, 4096, false, true, DIR, NB>(a, sm, tw, t);
+        fft_pass<M, 16, 1, true, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 16, false, false, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
+        fft_pass<M, 16, 256, false, false, DIR, NB, Sync>(a, sm, tw, t, &p2, sync);
+        fft_pass<M, 2, 4096, false, true, DIR, NB, Sync>(a, sm, tw, t, nullptr, sync);
     }
 }
 

@@ -108,10 +108,10 @@ __device__ __forceinline__ float2 fold_at(const HarmPlan& H, int z, int half, in
 // transforms and leave p[e] = (power of even output, power of odd output)
 // at m = t + e*M/16.  The templates carry the 1/L normalisation, so |y|^2
 // is the power.
-template <int M, bool F16, bool SPLIT>
+template <int M, bool F16, bool SPLIT, class Sync = CtaSync>
 __device__ __forceinline__ void plane_powers(const HarmPlan& H, const float2* __restrict__ D, int z,
                                              float2* sm, const float2* __restrict__ tw, float2 (&p)[16],
-                                             int t) {
+                                             int t, Sync sync = Sync()) {
     static_assert(!SPLIT, "the sequential layout stores each transform as it completes");
     constexpr int T = M / 16;
     float2 x[2][16];
@@ -122,7 +122,7 @@ __device__ __forceinline__ void plane_powers(const HarmPlan& H, const float2* __
         x[0][e] = cmul(d, fold_at<M, F16>(H, z, 0, idx));
         x[1][e] = cmul(d, fold_at<M, F16>(H, z, 1, idx));
     }
-    fft_run<M, +1, 2>(x, sm, tw, t);
+    fft_run<M, +1, 2, Sync>(x, sm, tw, t, sync);
 #pragma unroll
     for (int e = 0; e < 16; e++)
         p[e] = make_float2(fmaf(x[0][e].x, x[0][e].x, x[0][e].y * x[0][e].y),
@@ -352,17 +352,24 @@ __host__ __device__ constexpr int stage_after(int h) {
     return ((h + 1) & h) ? -1 : (h == 0 ? 0 : h == 1 ? 1 : h == 3 ? 2 : h == 7 ? 3 : 4);
 }
 
+// Static shared memory of one harmonic-sum tile.
+template <int NH> struct TileShared {
+    int row[NH][kTileZ];  // byte offset of the row used by tile row zr
+    int zf[NH], nzr[NH], r0[NH], c0[NH], w4[NH], off[NH];
+    int cb[NH], crem[NH];  // column of tile column 0, and the rounding remainder
+};
+
+// One tile: segment seg, f-dot rows [z0, z0 + kTileZ), columns [i0, i0 +
+// kTileI), by the CTA's kTileI threads.  The CTA's mbarrier `bar` is
+// initialised here when init is set (its first use), else reused: the
+// caller passes the parity of this use.  Returns false -- with the error
+// word set -- when the copies did not land within the bounded wait; the
+// barrier's state is then unknown and the CTA must not use it again.
 template <int NH, bool STAGE_OUT>
-__global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
+__device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z0, int i0, float* tsm,
+                                               TileShared<NH>& S, unsigned long long* bar, bool init,
+                                               unsigned parity) {
     static_assert(NH <= 32, "one lane per harmonic");
-    extern __shared__ __align__(128) float tsm[];
-    __shared__ __align__(16) int s_row[NH][kTileZ];  // byte offset of the row used by tile row zr
-    __shared__ int s_zf[NH], s_nzr[NH], s_r0[NH], s_c0[NH], s_w4[NH], s_off[NH];
-    __shared__ int s_cb[NH], s_crem[NH];  // column of tile column 0, and the rounding remainder
-    __shared__ __align__(8) unsigned long long s_bar;
-    const int seg = blockIdx.z;
-    const int z0 = blockIdx.y * kTileZ;
-    const int i0 = blockIdx.x * kTileI;
     const int nz = min(kTileZ, a.numzs0 - z0);
     const int ni = min(kTileI, a.uselen - i0);
     const long long startr = a.segs[seg].startr;
@@ -391,18 +398,18 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
             const int c0 = rfirst & ~3;
             const int w4 = ((rlast - c0) >> 2) + 1;
             nzr = zl - zf + 1;
-            s_zf[h] = zf;
-            s_nzr[h] = nzr;
-            s_c0[h] = c0;
-            s_w4[h] = w4;
+            S.zf[h] = zf;
+            S.nzr[h] = nzr;
+            S.c0[h] = c0;
+            S.w4[h] = w4;
             size = 4 * nzr * w4;
             // twice_r_shift(2 startr + i0 + k) = (B + 2 k p) >> (lq + 1) with
             // B = 2 (2 startr + i0) p + 2^lq: split B once so that every
             // thread finishes in 32 bits (only the low 16 bits of the
             // difference to rlo2 matter, as in the reference's ushort)
             const long long B = 2LL * (2 * startr + i0) * H.p + (1LL << H.lq);
-            s_cb[h] = (int)((B >> (H.lq + 1)) - rlo2) - c0;
-            s_crem[h] = (int)(B & ((2LL << H.lq) - 1));
+            S.cb[h] = (int)((B >> (H.lq + 1)) - rlo2) - c0;
+            S.crem[h] = (int)(B & ((2LL << H.lq) - 1));
         }
         int incl = size, rincl = nzr;
 #pragma unroll
@@ -415,25 +422,25 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
             }
         }
         if (tid < NH) {
-            s_off[tid] = incl - size;
-            s_r0[tid] = rincl - nzr;  // first copy index of harmonic tid
+            S.off[tid] = incl - size;
+            S.r0[tid] = rincl - nzr;  // first copy index of harmonic tid
         }
         const int total_floats = __shfl_sync(0xffffffffu, incl, 31);
         const int total_rows = __shfl_sync(0xffffffffu, rincl, 31);
         if (tid == 0) {
-            mbar_init(&s_bar, 1);
-            mbar_arrive_expect_tx(&s_bar, 4u * (unsigned)total_floats + a.test_extra_tx);
+            if (init) mbar_init(bar, 1);
+            mbar_arrive_expect_tx(bar, 4u * (unsigned)total_floats + a.test_extra_tx);
         }
         __syncwarp();
         for (int j = tid; j < total_rows; j += 32) {
             int h = 0;
 #pragma unroll
             for (int g = 1; g < NH; g++)
-                if (j >= s_r0[g]) h = g;
+                if (j >= S.r0[g]) h = g;
             const HarmPlan& H = a.h[h];
-            const int r = j - s_r0[h], w4 = s_w4[h];
-            bulk_copy_g2s(tsm + s_off[h] + 4 * w4 * r, P + H.poff + (long long)(s_zf[h] + r) * H.prow + s_c0[h],
-                          16u * (unsigned)w4, &s_bar);
+            const int r = j - S.r0[h], w4 = S.w4[h];
+            bulk_copy_g2s(tsm + S.off[h] + 4 * w4 * r, P + H.poff + (long long)(S.zf[h] + r) * H.prow + S.c0[h],
+                          16u * (unsigned)w4, bar);
         }
     }
     __syncthreads();
@@ -443,8 +450,8 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
 #pragma unroll
     for (int h = 0; h < NH; h++) {
         if (tid < kTileZ) {
-            const int r = (tid >= nz) ? 0 : (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - s_zf[h];
-            s_row[h][tid] = 4 * (s_off[h] + 4 * s_w4[h] * r);
+            const int r = (tid >= nz) ? 0 : (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - S.zf[h];
+            S.row[h][tid] = 4 * (S.off[h] + 4 * S.w4[h] * r);
         }
     }
     int colb[NH];  // byte offset of this thread's column
@@ -454,8 +461,8 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
             colb[h] = valid ? 4 * tid : 0;  // lanes past the plane edge read column 0
         } else {
             const HarmPlan& H = a.h[h];
-            const int c0 = s_c0[h];
-            const int rind = (unsigned short)(s_cb[h] + c0 + ((s_crem[h] + 2 * tid * H.p) >> (H.lq + 1)));
+            const int c0 = S.c0[h];
+            const int rind = (unsigned short)(S.cb[h] + c0 + ((S.crem[h] + 2 * tid * H.p) >> (H.lq + 1)));
             colb[h] = valid ? 4 * (rind - c0) : 0;
         }
     }
@@ -463,11 +470,11 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
 #pragma unroll
     for (int st = 0; st < kMaxStages; st++) cut[st] = a.cut[st];
     // 3. wait for the copies (bounded; every thread agrees on the outcome)
-    const bool landed = mbar_wait_bounded(&s_bar, 0);
+    const bool landed = mbar_wait_bounded(bar, parity);
     if (!__syncthreads_and(landed)) {
         if (tid == 0) atomicOr(a.err, 1ull);
-        mbar_wait_bounded(&s_bar, 0);  // give copies still in flight a last chance to land
-        return;
+        mbar_wait_bounded(bar, parity);  // give copies still in flight a last chance to land
+        return false;
     }
 
     // 4. sums in the reference's harmonic order, RB rows at a time (their
@@ -482,13 +489,13 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
 #pragma unroll
         for (int h = 0; h < NH; h++) {
             if constexpr (RB == 4) {
-                const int4 v = *reinterpret_cast<const int4*>(&s_row[h][zq]);
+                const int4 v = *reinterpret_cast<const int4*>(&S.row[h][zq]);
                 ro[h][0] = v.x;
                 ro[h][1] = v.y;
                 ro[h][2] = v.z;
                 ro[h][3] = v.w;
             } else {
-                const int2 v = *reinterpret_cast<const int2*>(&s_row[h][zq]);
+                const int2 v = *reinterpret_cast<const int2*>(&S.row[h][zq]);
                 ro[h][0] = v.x;
                 ro[h][1] = v.y;
             }
@@ -525,6 +532,16 @@ __global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
             }
         }
     }
+    return true;
+}
+
+template <int NH, bool STAGE_OUT>
+__global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
+    extern __shared__ __align__(128) float tsm[];
+    __shared__ __align__(16) TileShared<NH> S;
+    __shared__ __align__(8) unsigned long long s_bar;
+    hsum_tile_body<NH, STAGE_OUT>(a, blockIdx.z, blockIdx.y * kTileZ, blockIdx.x * kTileI, tsm, S, &s_bar, true,
+                                  0u);
 }
 
 // ------------------------------------------------------- pipelined tiled hsum

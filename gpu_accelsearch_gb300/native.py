@@ -58,7 +58,7 @@ class ServerStats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("chunk_segments", C.c_int), ("plane_split", C.c_int), ("fused_sum", C.c_int),
                 ("hsum_rowwise", C.c_int), ("serial_sum", C.c_int), ("hsum_pipelined", C.c_int),
-                ("graph", C.c_int), ("wait_test", C.c_int)]
+                ("graph", C.c_int), ("persistent", C.c_int), ("wait_test", C.c_int)]
 
 
 class Optimized(C.Structure):
@@ -75,13 +75,13 @@ class FilterbankInfo(C.Structure):
 
 
 class Stats(C.Structure):
-    _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 6),
-                ("kind_ms", C.c_double * 6), ("segments", C.c_longlong),
+    _fields_ = [("launches", C.c_longlong), ("kind_launches", C.c_longlong * 7),
+                ("kind_ms", C.c_double * 7), ("segments", C.c_longlong),
                 ("cells", C.c_longlong), ("search_ms", C.c_double), ("searches", C.c_longlong),
                 ("graph_launches", C.c_longlong), ("graph_builds", C.c_longlong)]
 
 
-KINDS = ["prep", "plane", "hsum", "whiten", "rfft", "fund"]
+KINDS = ["prep", "plane", "hsum", "whiten", "rfft", "fund", "step"]
 
 _vp, _ll, _llp = C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)
 SIGNATURES = {

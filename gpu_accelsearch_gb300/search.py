@@ -197,11 +197,12 @@ class AccelSearch:
         return {"chunk_segments": t.chunk_segments, "plane_split": t.plane_split,
                 "fused_sum": t.fused_sum,
                 "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum,
-                "hsum_pipelined": t.hsum_pipelined, "graph": t.graph, "wait_test": t.wait_test}
+                "hsum_pipelined": t.hsum_pipelined, "graph": t.graph, "wait_test": t.wait_test,
+                "persistent": t.persistent}
 
     def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
                    hsum_rowwise=None, serial_sum=None, hsum_pipelined=None, graph=None,
-                   wait_test=None):
+                   wait_test=None, persistent=None):
         cur = self.tuning()
         t = N.Tuning()
         t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
@@ -212,6 +213,7 @@ class AccelSearch:
         t.hsum_pipelined = cur["hsum_pipelined"] if hsum_pipelined is None else int(hsum_pipelined)
         t.graph = cur["graph"] if graph is None else int(graph)
         t.wait_test = cur["wait_test"] if wait_test is None else int(wait_test)
+        t.persistent = cur["persistent"] if persistent is None else int(persistent)
         N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
 
     def profile(self, enable: bool = True):

@@ -75,10 +75,11 @@ typedef struct accel_candidate {
 } accel_candidate;
 
 /* Kernel accounting of a context (accel_get_stats).  Kinds: 0 segment
- * preparation, 1 power planes, 2 harmonic sum (stage API), 3 whitening,
- * 4 R2C FFT (cuFFT; not counted in `launches`), 5 fundamental plane fused
- * with the harmonic sum (search path). */
-#define ACCEL_KINDS 6
+ * preparation, 1 power planes, 2 harmonic sum, 3 whitening, 4 R2C FFT
+ * (cuFFT; not counted in `launches`), 5 fundamental plane fused with the
+ * harmonic sum, 6 power planes and harmonic sums of a launch group in one
+ * persistent launch (accel_tuning.persistent). */
+#define ACCEL_KINDS 7
 typedef struct accel_stats {
     long long launches;                 /* kernels of this library launched   */
     long long kind_launches[ACCEL_KINDS];
@@ -116,6 +117,12 @@ typedef struct accel_tuning {
                             /* sequence keeps its shape); 0: direct launches. */
                             /* Searches that copy series from host memory     */
                             /* always launch directly                         */
+    int persistent;         /* 1: a launch group's plane rows and harmonic-sum */
+                            /* tiles run in one persistent launch from one    */
+                            /* work queue, each segment summed as soon as its */
+                            /* rows are written (still in L2); segment lengths*/
+                            /* other than 8192 and plans it cannot take fall  */
+                            /* back to the separate kernels                   */
     int wait_test;          /* failure-detection test, 0 in normal use: each  */
                             /* tile of the tiled harmonic sum expects 16      */
                             /* bytes that never arrive, so its bounded copy   */
