@@ -195,6 +195,14 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
         srv.wait(rid, -1)
         lats.append(srv.result(rid)[1])
     wall = time.perf_counter() - t0
+    # latency by length class (octaves of the sample count)
+    by_class = {}
+    for (ta, x, z), lat in zip(arrivals, lats):
+        k = int(np.floor(np.log2(x.size)))
+        by_class.setdefault(k, []).append(lat)
+    classes = {f"2^{k}..2^{k + 1}": {"requests": len(v), "p50_ms": float(np.percentile(v, 50)),
+                                      "p99_ms": float(np.percentile(v, 99))}
+               for k, v in sorted(by_class.items())}
     st = srv.stats()
     srv.close()
     cells = st["cells"] - base["cells"]
@@ -204,9 +212,9 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
             "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
             "mean_ms": float(lats.mean()), "max_ms": float(lats.max()),
             "cells_per_s": cells / wall, "cells_per_gpu_s": cells / gpu_s if gpu_s else None,
-            "worker_admit_s": (st["admit_ms"] - base["admit_ms"]) / 1e3,
-            "worker_group_s": (st["group_ms"] - base["group_ms"]) / 1e3,
-            "wall_s": wall, "hbm_budget_bytes": 150e9,
+            "admission_thread_s": (st["admit_ms"] - base["admit_ms"]) / 1e3,
+            "scheduler_group_s": (st["group_ms"] - base["group_ms"]) / 1e3,
+            "wall_s": wall, "hbm_budget_bytes": 150e9, "max_wait_s": 1.0, "by_length": classes,
             "workload": "Poisson arrivals, lengths log-uniform 2^18..2^23 (rounded up to even "
                         "7-smooth lengths), "
                         "zmax uniform in {50,100,200,300}, 5% with a signal, L=8192, 8 harmonics, "

@@ -1,20 +1,28 @@
 // server.cu -- continuous-batching request server (accel_server_*).
 //
-// Requests are single DM-trial time series.  A scheduler thread
-//   * admits queued requests in arrival order, as their R2C plans are
-//     ready, while their device memory (series + spectrum) fits the HBM
-//     budget and the active limit, copies the series in, and runs the R2C
-//     transform and whitening on the device;
-//   * builds each launch group from the active requests of one template
-//     bank (one bank per zmax, created on first use), shortest remaining
-//     work first: the bank holding the active request with the least work
-//     left, then that bank's requests in order of remaining steps, as many
-//     steps of each as the group has room for.  A request admitted while
+// Requests are single DM-trial time series.
+//   * An admission thread admits queued requests in arrival order, as their
+//     R2C plans are ready, while their device memory (series + spectrum)
+//     fits the HBM budget and the active limit: it copies the series in and
+//     runs the R2C transform and whitening on its own stream, records an
+//     event and hands the request to the scheduler.  (Copies from pageable
+//     host memory block the calling thread; on their own thread they no
+//     longer hold up the launches.)
+//   * The scheduler thread orders its stream after each handed-over
+//     request's event and builds each launch group from the active requests
+//     of one template bank (one bank per zmax, created on first use),
+//     shortest remaining work first -- the bank holding the request with
+//     the least work left, then that bank's requests in the same order, as
+//     many steps of each as the group has room for -- except that while
+//     requests have waited longer than max_wait_s since submission, every
+//     other group serves them first, oldest first.  A request admitted while
 //     others are in flight joins the very next group that has room, so its
-//     work overlaps with theirs on the device, and a short request overtakes
-//     a long one instead of sharing the GPU with it step by step;
-//   * launches the next group before it reads back the previous one (two
-//     buffer sets per bank), and completes a request when its last step
+//     work overlaps with theirs on the device; a short request overtakes a
+//     long one instead of sharing the GPU with it step by step, and the
+//     wait limit keeps long requests from starving while arrivals continue;
+//   * keeps further launch groups queued on the GPU while it reads back
+//     the oldest (kFlightDepth in flight, one buffer set more per bank),
+//     and completes a request when its last step
 //     has been summed: candidates are kept for accel_server_result, its
 //     device memory is released and its latency (submission to completion)
 //     recorded.
@@ -46,6 +54,10 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Launch groups launched and not yet read back: the host reads the oldest
+// once this many are queued, so the GPU still has the others to run.
+constexpr int kFlightDepth = 3;
+
 struct Request {
     long long id = 0;
     const float* host = nullptr;
@@ -58,6 +70,7 @@ struct Request {
     double bytes = 0;
     int state = 0;  // 0 queued, 1 active, 2 done, 3 failed
     int rc = ACCEL_OK;
+    cudaEvent_t ready = nullptr;  // end of its copy, R2C and whitening (admission stream)
     std::vector<accel_candidate> cands;
     Clock::time_point t_submit, t_done;
 };
@@ -76,7 +89,7 @@ struct GroupBuf {
 struct Group {
     accel_ctx* ctx = nullptr;
     std::vector<Request*> active;
-    GroupBuf buf[2];  // launch groups of this bank alternate between them
+    GroupBuf buf[kFlightDepth + 1];  // launch groups of this bank take them in turn
     int next_buf = 0;
 };
 
@@ -99,8 +112,12 @@ constexpr int kPlanners = 4;
 
 struct accel_server {
     accel_server_config cfg{};
-    cudaStream_t stream = nullptr;
-    std::thread worker;
+    cudaStream_t stream = nullptr;   // launch groups (scheduler thread)
+    cudaStream_t astream = nullptr;  // copies, R2C and whitening (admission thread)
+    accel_ctx* wctx = nullptr;       // whitening plans of the admission thread
+    std::thread worker, admitter;
+    bool admitter_done = false;
+    std::deque<Request*> ready;      // admitted and prepared, not yet with the scheduler
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     bool stop = false;
@@ -122,8 +139,8 @@ struct accel_server {
     size_t work_bytes = 0;
     double bytes_in_use = 0;
     accel_server_stats st{};
-    Flight flight;           // at most one group in flight while the next is built
-    bool in_flight = false;
+    std::deque<Flight> flights;  // launched groups not yet read back, oldest first
+    bool late_turn = true;       // the next group serves the late requests (when there are any)
 };
 
 namespace {
@@ -143,9 +160,11 @@ void release_plan(accel_server* s, long long n) {
     if (wake) s->plan_cv.notify_all();
 }
 
-void finish(accel_server* s, Request* r, int rc) {
-    if (r->d_series) cudaFreeAsync(r->d_series, s->stream);
-    if (r->d_spec) cudaFreeAsync(r->d_spec, s->stream);
+void finish(accel_server* s, Request* r, int rc, cudaStream_t st) {
+    if (r->d_series) cudaFreeAsync(r->d_series, st);
+    if (r->d_spec) cudaFreeAsync(r->d_spec, st);
+    if (r->ready) cudaEventDestroy(r->ready);
+    r->ready = nullptr;
     r->d_series = nullptr;
     r->d_spec = nullptr;
     release_plan(s, r->n);
@@ -157,6 +176,7 @@ void finish(accel_server* s, Request* r, int rc) {
     s->st.completed++;
     s->st.active--;
     s->cv_done.notify_all();
+    s->cv_work.notify_all();  // budget freed: the admission thread may admit more
 }
 
 void free_group(Group& g) {
@@ -214,15 +234,14 @@ accel_ctx* group_ctx(accel_server* s, int zmax, int* rc) {
 }
 
 
-// Copy in, transform and whiten one admitted request (worker thread).
+// Copy in, transform and whiten one admitted request (admission thread,
+// admission stream), then record its event.
 int admit(accel_server* s, Request* r) {
     int rc = ACCEL_OK;
-    accel_ctx* c = group_ctx(s, r->zmax, &rc);
-    if (!c) return rc;
-    if (cudaMallocAsync(&r->d_series, sizeof(float) * r->n, s->stream) != cudaSuccess ||
-        cudaMallocAsync(&r->d_spec, sizeof(float2) * (r->n / 2 + 1), s->stream) != cudaSuccess)
+    if (cudaMallocAsync(&r->d_series, sizeof(float) * r->n, s->astream) != cudaSuccess ||
+        cudaMallocAsync(&r->d_spec, sizeof(float2) * (r->n / 2 + 1), s->astream) != cudaSuccess)
         return set_error(ACCEL_ERR_NOMEM, "request %lld: device allocation", r->id);
-    if (cudaMemcpyAsync(r->d_series, r->host, sizeof(float) * r->n, cudaMemcpyHostToDevice, s->stream) !=
+    if (cudaMemcpyAsync(r->d_series, r->host, sizeof(float) * r->n, cudaMemcpyHostToDevice, s->astream) !=
         cudaSuccess)
         return set_error(ACCEL_ERR_CUDA, "request %lld: copy", r->id);
     R2CPlan pl;
@@ -234,7 +253,7 @@ int admit(accel_server* s, Request* r) {
     if (!pl.ok) return set_error(ACCEL_ERR_CUDA, "request %lld: cuFFT plan for %lld samples", r->id, r->n);
     if (pl.work > s->work_bytes) {
         // grow the shared work area (transforms in flight use the old one)
-        if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        if (cudaStreamSynchronize(s->astream) != cudaSuccess)
             return set_error(ACCEL_ERR_CUDA, "request %lld: stream", r->id);
         cudaFree(s->work);
         s->work = nullptr;
@@ -243,16 +262,38 @@ int admit(accel_server* s, Request* r) {
             return set_error(ACCEL_ERR_NOMEM, "request %lld: cuFFT work area", r->id);
         s->work_bytes = pl.work;
     }
-    if (cufftSetWorkArea(pl.plan, s->work) != CUFFT_SUCCESS || cufftSetStream(pl.plan, s->stream) != CUFFT_SUCCESS ||
+    if (cufftSetWorkArea(pl.plan, s->work) != CUFFT_SUCCESS || cufftSetStream(pl.plan, s->astream) != CUFFT_SUCCESS ||
         cufftExecR2C(pl.plan, r->d_series, reinterpret_cast<cufftComplex*>(r->d_spec)) != CUFFT_SUCCESS)
         return set_error(ACCEL_ERR_CUDA, "request %lld: R2C", r->id);
-    rc = do_whiten(c, r->d_spec, (unsigned)r->numbins);
-    if (!rc) {
-        const long long half = (unsigned short)(c->uselen / 2);
-        r->nsteps = 0;
-        for (long long x = r->rlo; x + half < r->numbins; x += half) r->nsteps++;
-    }
+    rc = do_whiten(s->wctx, r->d_spec, (unsigned)r->numbins);
+    if (!rc && (cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventRecord(r->ready, s->astream) != cudaSuccess))
+        rc = set_error(ACCEL_ERR_CUDA, "request %lld: event", r->id);
     return rc;
+}
+
+// Scheduling order.  late_first: requests past the wait limit first,
+// oldest first, then the least work left (steps x fundamental cells per
+// step); otherwise the least work left for every request.  Ties by
+// submission.
+struct Prio {
+    bool late;
+    double key;
+    long long id;
+    bool operator<(const Prio& o) const {
+        if (late != o.late) return late;
+        if (key != o.key) return key < o.key;
+        return id < o.id;
+    }
+};
+bool is_late(const accel_server* s, const Request* r, Clock::time_point now) {
+    const double lim = s->cfg.max_wait_s > 0 ? s->cfg.max_wait_s : 1.0;
+    return std::chrono::duration<double>(now - r->t_submit).count() > lim;
+}
+Prio prio(const accel_server* s, const Request* r, const accel_ctx* c, Clock::time_point now, bool late_first) {
+    if (late_first && is_late(s, r, now))
+        return Prio{true, -std::chrono::duration<double>(now - r->t_submit).count(), r->id};
+    return Prio{false, (double)(r->nsteps - r->next_step) * c->uselen * c->numzs0, r->id};
 }
 
 // Build and launch one group from the active requests of bank zmax:
@@ -260,7 +301,7 @@ int admit(accel_server* s, Request* r) {
 // a request before the next one's.  The candidate count is copied back
 // asynchronously; complete_group reads the rest.  Returns a flight with
 // n == 0 when the bank had no step left to issue.
-Flight launch_group(accel_server* s, int zmax) {
+Flight launch_group(accel_server* s, int zmax, bool late_first) {
     Flight f;
     f.zmax = zmax;
     Group& g = s->groups[zmax];
@@ -271,8 +312,9 @@ Flight launch_group(accel_server* s, int zmax) {
     const int cap = c->chunk;
     const long long half = (unsigned short)(c->uselen / 2);
     std::vector<Request*> order(g.active);
-    std::stable_sort(order.begin(), order.end(), [](const Request* a, const Request* b) {
-        return a->nsteps - a->next_step < b->nsteps - b->next_step;
+    const auto now = Clock::now();
+    std::stable_sort(order.begin(), order.end(), [&](const Request* a, const Request* b) {
+        return prio(s, a, c, now, late_first) < prio(s, b, c, now, late_first);
     });
     for (Request* r : order) {
         while ((int)f.owner.size() < cap && r->next_step < r->nsteps) {
@@ -288,7 +330,7 @@ Flight launch_group(accel_server* s, int zmax) {
     }
     f.n = (int)f.owner.size();
     if (f.n == 0) return f;
-    g.next_buf ^= 1;
+    g.next_buf = (g.next_buf + 1) % (kFlightDepth + 1);
     if (cudaMemcpyAsync(B.d_segs, B.h_segs, sizeof(SegDesc) * f.n, cudaMemcpyHostToDevice, s->stream) ||
         cudaMemsetAsync(B.d_ncand, 0, 2 * sizeof(unsigned long long), s->stream))
         f.rc = set_error(ACCEL_ERR_CUDA, "server: group upload");
@@ -351,7 +393,7 @@ void complete_group(accel_server* s, Flight& f) {
         Request* r = so.first;
         if (r->state != 1) continue;
         if (rc != ACCEL_OK) {
-            finish(s, r, rc);
+            finish(s, r, rc, s->stream);
             continue;
         }
         if (++r->done_steps == r->nsteps) {
@@ -361,7 +403,7 @@ void complete_group(accel_server* s, Flight& f) {
                 if (a.z != b.z) return a.z < b.z;
                 return a.r < b.r;
             });
-            finish(s, r, ACCEL_OK);
+            finish(s, r, ACCEL_OK, s->stream);
         }
     }
     std::vector<Request*> keep;
@@ -418,35 +460,36 @@ void planner_loop(accel_server* s) {
     }
 }
 
-void worker_loop(accel_server* s) {
+// Admission thread: admits queued requests in arrival order as their R2C
+// plans become ready (a request whose plan is still being made does not
+// hold back the ones behind it) while the HBM budget and the active limit
+// allow, stopping at the first request they cannot take; prepares each
+// on the admission stream and hands it to the scheduler.
+void admitter_loop(accel_server* s) {
     cudaSetDevice(s->cfg.device);
     for (;;) {
         std::vector<Request*> admitted;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            // queued requests are admitted in arrival order as their R2C
-            // plans become ready (a request whose plan is still being made
-            // does not hold back the ones behind it); admission stops at
-            // the first request the HBM budget or the active limit cannot
-            // take (lock order: mu, then plan_mu)
+            // lock order: mu, then plan_mu
             auto plan_ready = [&](const Request* r) {
                 std::lock_guard<std::mutex> pk(s->plan_mu);
                 return s->plans.count(r->n) != 0;
             };
-            auto any_ready = [&] {
-                for (const Request* r : s->pending)
+            auto can_admit = [&] {
+                for (const Request* r : s->pending) {
+                    if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) return false;
+                    if (s->bytes_in_use + r->bytes > s->cfg.hbm_budget_bytes) return false;
                     if (plan_ready(r)) return true;
+                }
                 return false;
             };
-            s->cv_work.wait(lk, [&] {
-                if (s->stop || s->in_flight || any_ready()) return true;
-                for (auto& kv : s->groups)
-                    if (!kv.second.active.empty()) return true;
-                return false;
-            });
-            bool any_active = false;
-            for (auto& kv : s->groups) any_active |= !kv.second.active.empty();
-            if (s->stop && s->pending.empty() && !any_active && !s->in_flight) return;
+            s->cv_work.wait(lk, [&] { return (s->stop && s->pending.empty()) || can_admit(); });
+            if (s->stop && s->pending.empty()) {
+                s->admitter_done = true;
+                s->cv_work.notify_all();
+                return;
+            }
             for (auto it = s->pending.begin(); it != s->pending.end();) {
                 Request* r = *it;
                 if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) break;
@@ -466,52 +509,99 @@ void worker_loop(accel_server* s) {
         }
         for (Request* r : admitted) {
             const auto ta = Clock::now();
-            int rc = admit(s, r);
+            const int rc = admit(s, r);
             {
                 const double ms = std::chrono::duration<double, std::milli>(Clock::now() - ta).count();
                 std::lock_guard<std::mutex> lk(s->mu);
                 s->st.admit_ms += ms;
             }
             if (rc) {
-                finish(s, r, rc);
+                finish(s, r, rc, s->astream);
                 continue;
             }
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->ready.push_back(r);
+            }
+            s->cv_work.notify_all();
+        }
+    }
+}
+
+// Scheduler thread: takes prepared requests, builds and launches groups.
+void worker_loop(accel_server* s) {
+    cudaSetDevice(s->cfg.device);
+    for (;;) {
+        std::vector<Request*> incoming;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] {
+                if (!s->flights.empty() || !s->ready.empty()) return true;
+                for (auto& kv : s->groups)
+                    if (!kv.second.active.empty()) return true;
+                return s->stop && s->admitter_done;
+            });
+            bool any_active = false;
+            for (auto& kv : s->groups) any_active |= !kv.second.active.empty();
+            if (s->stop && s->admitter_done && s->ready.empty() && !any_active && s->flights.empty()) return;
+            incoming.assign(s->ready.begin(), s->ready.end());
+            s->ready.clear();
+        }
+        for (Request* r : incoming) {
+            int rc = ACCEL_OK;
+            accel_ctx* c = group_ctx(s, r->zmax, &rc);
+            // the group stream waits for the request's copy, R2C and whitening
+            if (c && cudaStreamWaitEvent(s->stream, r->ready, 0) != cudaSuccess)
+                rc = set_error(ACCEL_ERR_CUDA, "request %lld: stream wait", r->id);
+            if (!c || rc) {
+                finish(s, r, rc ? rc : ACCEL_ERR_CUDA, s->stream);
+                continue;
+            }
+            const long long half = (unsigned short)(c->uselen / 2);
+            r->nsteps = 0;
+            for (long long x = r->rlo; x + half < r->numbins; x += half) r->nsteps++;
             if (r->nsteps == 0) {
-                finish(s, r, ACCEL_OK);
+                finish(s, r, ACCEL_OK, s->stream);
                 continue;
             }
             s->groups[r->zmax].active.push_back(r);
         }
-        // the bank holding the active request with the least work left
-        // (steps x fundamental cells per step; ties: earlier submission)
+        // while requests past the wait limit exist, every other launch
+        // group serves them (oldest first) and the others stay shortest
+        // remaining work first: late requests get at least half of the GPU
+        // and short ones keep flowing
         int zmax = -1;
-        double best = 0.0;
-        long long best_id = 0;
+        Prio best{};
+        const auto now = Clock::now();
+        bool any_late = false;
+        for (auto& kv : s->groups)
+            for (Request* r : kv.second.active)
+                any_late |= r->next_step < r->nsteps && is_late(s, r, now);
+        const bool late_first = any_late && s->late_turn;
+        if (any_late) s->late_turn = !s->late_turn;
         for (auto& kv : s->groups) {
             accel_ctx* c = kv.second.ctx;
             for (Request* r : kv.second.active) {
                 if (r->next_step >= r->nsteps) continue;
-                const double w = (double)(r->nsteps - r->next_step) * c->uselen * c->numzs0;
-                if (zmax < 0 || w < best || (w == best && r->id < best_id)) {
+                const Prio p = prio(s, r, c, now, late_first);
+                if (zmax < 0 || p < best) {
                     zmax = kv.first;
-                    best = w;
-                    best_id = r->id;
+                    best = p;
                 }
             }
         }
-        // launch the next group, then read back the one before it: the
-        // host's candidate handling and the next group's set-up overlap the
+        // launch the next group, then read back the oldest one once
+        // kFlightDepth are queued (or nothing new could be launched): the
+        // host's candidate handling and the next groups' set-up overlap the
         // GPU's work
         const auto tg = Clock::now();
         Flight next;
-        if (zmax >= 0) next = launch_group(s, zmax);
-        if (s->in_flight) {
-            complete_group(s, s->flight);
-            s->in_flight = false;
-        }
-        if (next.n > 0) {
-            s->flight = std::move(next);
-            s->in_flight = true;
+        if (zmax >= 0) next = launch_group(s, zmax, late_first);
+        const bool launched = next.n > 0;
+        if (launched) s->flights.push_back(std::move(next));
+        if (!s->flights.empty() && ((int)s->flights.size() >= kFlightDepth || !launched)) {
+            complete_group(s, s->flights.front());
+            s->flights.pop_front();
         }
         {
             const double ms = std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
@@ -535,6 +625,7 @@ void accel_server_config_init(accel_server_config* c) {
     c->sigma = 6.0;
     c->chunk_segments = 128;
     c->device = 0;
+    c->max_wait_s = 1.0;
 }
 
 int accel_server_create(const accel_server_config* cfg, accel_server** out) {
@@ -544,13 +635,35 @@ int accel_server_create(const accel_server_config* cfg, accel_server** out) {
     accel_server* s = new accel_server();
     s->cfg = *cfg;
     if (s->cfg.chunk_segments <= 0) s->cfg.chunk_segments = 128;
+    if (!(s->cfg.max_wait_s > 0)) s->cfg.max_wait_s = 1.0;
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->astream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
+        if (s->stream) cudaStreamDestroy(s->stream);
         delete s;
         return set_error(ACCEL_ERR_CUDA, "accel_server_create: %s", cudaGetErrorString(e));
     }
+    // whitening for the admission thread: a context of its own (its plans
+    // cache is not shared with the scheduler's contexts), on its stream
+    accel_config wc;
+    accel_config_init(&wc);
+    wc.zmax = 0;
+    wc.numharm = 1;
+    wc.fftlen = 128;
+    wc.chunk_segments = 1;
+    wc.device = cfg->device;
+    int rc = accel_create(&wc, &s->wctx);
+    if (!rc) rc = accel_set_stream(s->wctx, s->astream);
+    if (rc) {
+        if (s->wctx) accel_destroy(s->wctx);
+        cudaStreamDestroy(s->astream);
+        cudaStreamDestroy(s->stream);
+        delete s;
+        return rc;
+    }
     for (int i = 0; i < kPlanners; i++) s->planners.emplace_back(planner_loop, s);
+    s->admitter = std::thread(admitter_loop, s);
     s->worker = std::thread(worker_loop, s);
     *out = s;
     return ACCEL_OK;
@@ -563,6 +676,7 @@ int accel_server_destroy(accel_server* s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
+    if (s->admitter.joinable()) s->admitter.join();
     if (s->worker.joinable()) s->worker.join();
     {
         std::lock_guard<std::mutex> lk(s->plan_mu);
@@ -573,6 +687,7 @@ int accel_server_destroy(accel_server* s) {
     for (std::thread& t : s->planners)
         if (t.joinable()) t.join();
     cudaStreamSynchronize(s->stream);
+    cudaStreamSynchronize(s->astream);
     for (auto& kv : s->plans)
         if (kv.second.ok) cufftDestroy(kv.second.plan);
     cudaFree(s->work);
@@ -580,7 +695,10 @@ int accel_server_destroy(accel_server* s) {
     for (auto& kv : s->reqs) {
         if (kv.second->d_series) cudaFree(kv.second->d_series);
         if (kv.second->d_spec) cudaFree(kv.second->d_spec);
+        if (kv.second->ready) cudaEventDestroy(kv.second->ready);
     }
+    accel_destroy(s->wctx);
+    cudaStreamDestroy(s->astream);
     cudaStreamDestroy(s->stream);
     delete s;
     return ACCEL_OK;

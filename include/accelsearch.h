@@ -301,14 +301,17 @@ int  accel_bank_spectra(const accel_ctx *ctx, int h, accel_complex *kstd, accel_
 /* ------------------------------------------------------------------ serving */
 /* A request server with continuous batching (no counterpart in the
  * reference, whose driver searches one trial per process run).  Planner
- * threads make each request's R2C plan when it is submitted; a worker
+ * threads make each request's R2C plan when it is submitted; an admission
  * thread admits requests in arrival order, as their plans are ready, while
  * their device memory (series and spectrum, 12 bytes per sample) fits
- * hbm_budget_bytes, transforms and whitens them, and fills each launch
- * group from one template bank (one bank per zmax, built on first use),
- * shortest remaining work first: a request admitted while others are in
- * flight joins the next group with room, and a short request overtakes a
- * long one.  The next group is launched before the previous one's
+ * hbm_budget_bytes, and copies, transforms and whitens them on its own
+ * stream; a scheduler thread fills each launch group from one template
+ * bank (one bank per zmax, built on first use), shortest remaining work
+ * first -- a request admitted while others are in flight joins the next
+ * group with room, and a short request overtakes a long one -- except that
+ * while requests have waited longer than max_wait_s, every other group
+ * serves them, oldest first, so that none starves while arrivals
+ * continue.  Further groups are launched before the oldest one's
  * candidates are read back.  A request's candidates do not depend on what
  * it was batched with. */
 typedef struct accel_server accel_server;
@@ -321,7 +324,10 @@ typedef struct accel_server_config {
     double sigma;             /* candidate threshold                           */
     int chunk_segments;       /* steps per launch group (0: 128)               */
     int device;
-    int reserved[8];
+    double max_wait_s;        /* requests waiting longer than this since their */
+                              /* submission get every other launch group,     */
+                              /* oldest first (0: 1.0 s)                       */
+    int reserved[6];
 } accel_server_config;
 
 typedef struct accel_server_stats {
@@ -329,8 +335,9 @@ typedef struct accel_server_stats {
     double bytes_in_use;      /* budgeted bytes of the admitted requests       */
     long long cells;          /* fundamental f-fdot cells searched             */
     double gpu_ms;            /* CUDA-event time of the launch groups          */
-    double admit_ms;          /* worker time admitting (copy, R2C, whitening)  */
-    double group_ms;          /* worker time running launch groups             */
+    double admit_ms;          /* admission-thread time (copy, R2C, whitening)  */
+    double group_ms;          /* scheduler time launching and completing groups */
+                              /* (includes waiting for the GPU)               */
 } accel_server_stats;
 
 void accel_server_config_init(accel_server_config *cfg);

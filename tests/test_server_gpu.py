@@ -100,3 +100,28 @@ def test_many_lengths_and_banks_equal_context_path():
         with AccelSearch(zmax=z, numharm=4, fftlen=2048) as s:
             s.search([x], DT)
             assert same(g, s.candidates()), (x.size, z)
+
+
+def test_wait_limit_bounds_a_long_request_under_a_flood_of_short_ones():
+    # 600 short requests queued behind one long request: shortest remaining
+    # work first alone would serve every short one first (~1.5 s of GPU
+    # work); with max_wait_s = 0.3 the long request gets every other launch
+    # group once it has waited 0.3 s, while short ones still overtake it
+    # before that
+    from gpu_accelsearch_gb300.serving import Server
+    long_x = synth_series(1 << 23, seed=30)
+    short_x = synth_series(1 << 20, seed=31)
+    with Server(hbm_budget_bytes=40e9, fftlen=8192, numharm=8, chunk_segments=128, max_wait_s=0.3) as srv:
+        assert srv.wait(srv.submit(short_x, DT, 200), 120)  # bank built before the measurement
+        lid = srv.submit(long_x, DT, 200)
+        sids = [srv.submit(short_x, DT, 200) for _ in range(600)]
+        assert srv.wait(lid, 300)
+        short_done_before = sum(1 for i in sids if srv.wait(i, 0.0))
+        for i in sids:
+            assert srv.wait(i, 300)
+        _, lat_long = srv.result(lid)
+        lat_short = [srv.result(i)[1] for i in sids]
+    assert short_done_before > 0          # shorter work still went first
+    assert short_done_before < len(sids)  # but not all of it: the wait limit cut in
+    assert lat_long < 0.3e3 + 0.7e3, lat_long  # limit + its own search and group latency
+    assert max(lat_short) > lat_long
