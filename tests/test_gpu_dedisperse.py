@@ -11,9 +11,20 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
+# the windowed kernel (channel windows in shared memory, 16 trials per CTA:
+# trial counts below, at and above a tile, channel counts that are not a
+# multiple of its 8-channel chunks, output lengths that end inside a tile),
+# and the one-load-per-addition kernel it falls back to when a tile's
+# delays spread too far for its windows (coarse DM steps: the first, third
+# and last two cases)
 @pytest.mark.parametrize("nchan,nsamp,dms", [(64, 30000, np.arange(0, 130, 10)),
                                              (7, 5000, [0.0, 3.5]),
-                                             (200, 9000, np.arange(0, 40, 2.5))])
+                                             (200, 9000, np.arange(0, 40, 2.5)),
+                                             (1027, 12000, np.arange(0, 33, 1.0)),
+                                             (256, 70000, np.arange(0, 64, 1.0)),
+                                             (64, 30000, np.arange(0, 20, 0.5)),
+                                             (96, 70000, np.arange(0, 1601, 100.0)),
+                                             (48, 400000, np.arange(0, 7001, 500.0))])
 def test_dedisperse_bit_exact(nchan, nsamp, dms):
     rng = np.random.default_rng(nchan)
     fb = rng.standard_normal((nchan, nsamp)).astype(np.float32)
