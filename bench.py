@@ -493,7 +493,7 @@ def run_ours(args):
         kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=1100, device=local)
         tuned = {"fftlen": kw["fftlen"], "chunk_segments": tun["chunk_segments"],
                  "plane_split": tun["plane_split"], "fused_sum": tun["fused_sum"],
-                 "sample_cells_per_s": rate}
+                 "hsum_tile_rows": tun["hsum_tile_rows"], "sample_cells_per_s": rate}
     fftlen = args.fftlen or tuned["fftlen"]
     chunk = args.chunk or tuned["chunk_segments"]
     split = args.split if args.split >= 0 else tuned["plane_split"]
@@ -501,6 +501,8 @@ def run_ours(args):
     extra = json.loads(args.tuning) if args.tuning else {}
     if tuned and "fused_sum" not in extra:
         extra["fused_sum"] = tuned["fused_sum"]
+    if tuned and "hsum_tile_rows" not in extra:
+        extra["hsum_tile_rows"] = tuned["hsum_tile_rows"]
     s.set_tuning(chunk_segments=chunk, plane_split=split, **extra)
     U, nz0 = s.uselen, s.harmonics[0].numzs
     nseg = sum(s.step_count(n, DT) for n in lengths)

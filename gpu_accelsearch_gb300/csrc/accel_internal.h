@@ -175,12 +175,16 @@ int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
-int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st);
+int launch_hsum_tile(const HsumArgs& a, int nseg, int tile_rows, cudaStream_t st);
 int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st);
 // Tile geometry of launch_hsum_tile (the host proves the shared-memory bound).
 constexpr int kHsumTileZ = 16;
 constexpr int kHsumTileI = 256;
 constexpr int kHsumTileFloats = 15360;
+// Shared-memory bound of a tile of tz f-dot rows (floats): 60 KB for 8 and
+// 16 rows, 112 KB for 32 (two CTAs per SM).
+constexpr int hsum_tile_floats_max(int tz) { return tz > 16 ? 28672 : kHsumTileFloats; }
+constexpr int kHsumTileRows[3] = {8, 16, 32};  // tile heights of launch_hsum_tile
 constexpr int kPipeBuffers = 4;   // tile buffers of the pipelined harmonic sum
 constexpr int kPipeSmemMax = 222 * 1024;  // their dynamic shared memory (227 KB less the static tables)
 

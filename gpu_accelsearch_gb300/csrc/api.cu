@@ -288,42 +288,48 @@ int build_plan(accel_ctx* c) {
             c->mvals.push_back(c->hp[h].M);
     for (int s = 0; s < c->nstages; s++)
         c->cuts[s] = (float)power_cut(c->cfg.sigma, 1 << s, c->cfg.numindep);
-    // Largest shared-memory footprint of a k_hsum_tile tile, over every tile
-    // position and every step phase (the geometry repeats with period q in
-    // startr), with the kernel's own index arithmetic.
-    int worst = 0, qmax = 1;
+    // Largest shared-memory footprint of a k_hsum_tile tile of each height,
+    // over every tile position and every step phase (the geometry repeats
+    // with period q in startr), with the kernel's own index arithmetic.
+    int qmax = 1;
     for (int h = 0; h < c->nh; h++) qmax = std::max(qmax, c->hp[h].q);
-    for (long long ph = 0; ph < 4LL * qmax; ph++) {
-        const long long startr = 1000000 + ph;
-        for (int z0 = 0; z0 < c->numzs0; z0 += kHsumTileZ) {
-            const int nz = std::min(kHsumTileZ, c->numzs0 - z0);
-            for (int i0 = 0; i0 < U; i0 += kHsumTileI) {
-                const int ni = std::min(kHsumTileI, U - i0);
-                int off = 0;
-                for (int h = 0; h < c->nh; h++) {
-                    const HarmPlan& H = c->hp[h];
-                    int rfirst = i0, rlast = i0 + ni - 1, zf = z0, zl = z0 + nz - 1;
-                    if (h > 0) {
-                        const long long rlo = twice_required_r(2 * startr, H.p, H.q) >> 1;
-                        rfirst = sub_rind(startr, i0, H.p, H.q, rlo);
-                        rlast = sub_rind(startr, i0 + ni - 1, H.p, H.q, rlo);
-                        zf = sub_zind(c->zlo0 + kDz * z0, H.p, H.q, H.zlo);
-                        zl = sub_zind(c->zlo0 + kDz * (z0 + nz - 1), H.p, H.q, H.zlo);
+    for (int k = 0; k < 3; k++) {
+        const int TZ = kHsumTileRows[k];
+        int worst = 0;
+        for (long long ph = 0; ph < 4LL * qmax && worst < (1 << 30); ph++) {
+            const long long startr = 1000000 + ph;
+            for (int z0 = 0; z0 < c->numzs0; z0 += TZ) {
+                const int nz = std::min(TZ, c->numzs0 - z0);
+                for (int i0 = 0; i0 < U; i0 += kHsumTileI) {
+                    const int ni = std::min(kHsumTileI, U - i0);
+                    int off = 0;
+                    for (int h = 0; h < c->nh; h++) {
+                        const HarmPlan& H = c->hp[h];
+                        int rfirst = i0, rlast = i0 + ni - 1, zf = z0, zl = z0 + nz - 1;
+                        if (h > 0) {
+                            const long long rlo = twice_required_r(2 * startr, H.p, H.q) >> 1;
+                            rfirst = sub_rind(startr, i0, H.p, H.q, rlo);
+                            rlast = sub_rind(startr, i0 + ni - 1, H.p, H.q, rlo);
+                            zf = sub_zind(c->zlo0 + kDz * z0, H.p, H.q, H.zlo);
+                            zl = sub_zind(c->zlo0 + kDz * (z0 + nz - 1), H.p, H.q, H.zlo);
+                        }
+                        const int c0 = rfirst & ~3;
+                        const int w4 = ((rlast - c0) >> 2) + 1;
+                        if (zl < zf || rlast < rfirst || zf < 0 || zl >= H.numzs || (rlast | 3) >= H.prow) {
+                            off = 1 << 30;  // never use the tiled kernel for this plan
+                            break;
+                        }
+                        off += 4 * (zl - zf + 1) * w4;
                     }
-                    const int c0 = rfirst & ~3;
-                    const int w4 = ((rlast - c0) >> 2) + 1;
-                    if (zl < zf || rlast < rfirst || zf < 0 || zl >= H.numzs || (rlast | 3) >= H.prow) {
-                        off = 1 << 30;  // never use the tiled kernel for this plan
-                        break;
-                    }
-                    off += 4 * (zl - zf + 1) * w4;
+                    worst = std::max(worst, off);
                 }
-                worst = std::max(worst, off);
             }
         }
+        c->tile_floats_h[k] = worst;
+        c->tile_ok_h[k] = worst <= hsum_tile_floats_max(TZ);
     }
-    c->tile_floats = worst;
-    c->tile_ok = worst <= kHsumTileFloats;
+    c->tile_floats = c->tile_floats_h[1];  // 16 rows: the pipelined and persistent sums
+    c->tile_ok = c->tile_ok_h[1];
     return ACCEL_OK;
 }
 
@@ -560,8 +566,13 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         c->stats.cells += (long long)nseg * c->uselen * c->numzs0;
         if (c->tile_ok && c->hsum_tiled && c->hsum_pipe && 4LL * ((c->tile_floats + 31) & ~31) * kPipeBuffers <= kPipeSmemMax)
             CKL(launch_hsum_pipe(ha, nseg, sum_stream), "harmonic sum (tiled, pipelined)");
-        else if (c->tile_ok && c->hsum_tiled)
-            CKL(launch_hsum_tile(ha, nseg, sum_stream), "harmonic sum (tiled)");
+        else if (c->tile_ok && c->hsum_tiled) {
+            // the tuned tile height where its tiles fit, else 16 rows
+            int k = c->tile_rows == 8 ? 0 : c->tile_rows == 32 ? 2 : 1;
+            if (!c->tile_ok_h[k]) k = 1;
+            ha.tile_floats = c->tile_floats_h[k];
+            CKL(launch_hsum_tile(ha, nseg, kHsumTileRows[k], sum_stream), "harmonic sum (tiled)");
+        }
         else
             CKL(launch_hsum(ha, nseg, sum_stream), "harmonic sum");
     }
@@ -1049,6 +1060,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->hsum_pipelined = c->hsum_pipe;
     t->graph = c->use_graph;
     t->persistent = c->persistent;
+    t->hsum_tile_rows = c->tile_rows;
     t->wait_test = c->wait_test;
     return ACCEL_OK;
 }
@@ -1057,6 +1069,8 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     if (!c || !t) return set_err(ACCEL_ERR_INVALID, "null argument");
     if (t->chunk_segments < 1 || t->chunk_segments > 65535)
         return set_err(ACCEL_ERR_INVALID, "chunk_segments must be in [1, 65535]");
+    if (t->hsum_tile_rows != 0 && t->hsum_tile_rows != 8 && t->hsum_tile_rows != 16 && t->hsum_tile_rows != 32)
+        return set_err(ACCEL_ERR_INVALID, "hsum_tile_rows must be 8, 16 or 32");
     int rc = ensure_device(c);
     if (rc) return rc;
     c->plane_split = t->plane_split != 0;
@@ -1066,6 +1080,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->hsum_pipe = t->hsum_pipelined != 0;
     c->use_graph = t->graph != 0;
     c->persistent = t->persistent != 0;
+    c->tile_rows = t->hsum_tile_rows ? t->hsum_tile_rows : 16;
     c->wait_test = t->wait_test != 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));

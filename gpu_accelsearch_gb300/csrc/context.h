@@ -79,6 +79,9 @@ struct accel_ctx {
     cudaStream_t gcap = nullptr, gcap2 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int tile_floats = 0;
+    int tile_floats_h[3] = {0, 0, 0};     // worst tile of 8, 16, 32 rows (floats)
+    bool tile_ok_h[3] = {false, false, false};
+    int tile_rows = 16;                   // height of the tiled sum's tiles
     float2* dbuf = nullptr;
     float* planes = nullptr;
     SegDesc* d_segs = nullptr;

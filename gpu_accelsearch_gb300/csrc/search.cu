@@ -32,20 +32,30 @@ int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int NH, bool SO>
+template <int NH, bool SO, int TZ>
 static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
     static std::atomic<unsigned long long> attr{0};
     int dev = 0;
     if (attr_pending(attr, &dev)) {
-        if (cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(float) * kTileSmemFloats)) != cudaSuccess ||
-            cudaFuncSetAttribute(k_hsum_tile<NH, SO>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        if (cudaFuncSetAttribute(k_hsum_tile<NH, SO, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(float) * hsum_tile_floats_max(TZ))) != cudaSuccess ||
+            cudaFuncSetAttribute(k_hsum_tile<NH, SO, TZ>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
         attr_set(attr, dev);
     }
-    k_hsum_tile<NH, SO><<<grid, kTileI, smem, st>>>(a);
+    k_hsum_tile<NH, SO, TZ><<<grid, kTileI, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NH, bool SO>
+static int hsum_tile_tz(const HsumArgs& a, int tz, dim3 grid, size_t smem, cudaStream_t st) {
+    switch (tz) {
+        case 8: return hsum_tile_nh<NH, SO, 8>(a, grid, smem, st);
+        case 16: return hsum_tile_nh<NH, SO, 16>(a, grid, smem, st);
+        case 32: return hsum_tile_nh<NH, SO, 32>(a, grid, smem, st);
+    }
+    return -1;
 }
 
 template <int NH, bool SO>
@@ -89,20 +99,21 @@ int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st) {
     return -1;
 }
 
-int launch_hsum_tile(const HsumArgs& a, int nseg, cudaStream_t st) {
-    dim3 grid((a.uselen + kTileI - 1) / kTileI, (a.numzs0 + kTileZ - 1) / kTileZ, nseg);
-    // the plan's own worst tile (at most kTileSmemFloats): a smaller
-    // footprint fits more CTAs per SM (4 instead of 3 at zmax 200, 8 harmonics)
-    const int floats = (a.tile_floats > 0 && a.tile_floats <= kTileSmemFloats) ? ((a.tile_floats + 3) & ~3)
-                                                                                : kTileSmemFloats;
+int launch_hsum_tile(const HsumArgs& a, int nseg, int tz, cudaStream_t st) {
+    dim3 grid((a.uselen + kTileI - 1) / kTileI, (a.numzs0 + tz - 1) / tz, nseg);
+    // the plan's own worst tile of this height (host-proven to fit): a
+    // smaller footprint fits more CTAs per SM (4 instead of 3 at zmax 200,
+    // 8 harmonics, 16 rows)
+    const int fmax = hsum_tile_floats_max(tz);
+    const int floats = (a.tile_floats > 0 && a.tile_floats <= fmax) ? ((a.tile_floats + 3) & ~3) : fmax;
     const size_t smem = sizeof(float) * floats;
     const bool so = a.stage_out != nullptr;
     switch (a.nh) {
-        case 1: return so ? hsum_tile_nh<1, true>(a, grid, smem, st) : hsum_tile_nh<1, false>(a, grid, smem, st);
-        case 2: return so ? hsum_tile_nh<2, true>(a, grid, smem, st) : hsum_tile_nh<2, false>(a, grid, smem, st);
-        case 4: return so ? hsum_tile_nh<4, true>(a, grid, smem, st) : hsum_tile_nh<4, false>(a, grid, smem, st);
-        case 8: return so ? hsum_tile_nh<8, true>(a, grid, smem, st) : hsum_tile_nh<8, false>(a, grid, smem, st);
-        case 16: return so ? hsum_tile_nh<16, true>(a, grid, smem, st) : hsum_tile_nh<16, false>(a, grid, smem, st);
+        case 1: return so ? hsum_tile_tz<1, true>(a, tz, grid, smem, st) : hsum_tile_tz<1, false>(a, tz, grid, smem, st);
+        case 2: return so ? hsum_tile_tz<2, true>(a, tz, grid, smem, st) : hsum_tile_tz<2, false>(a, tz, grid, smem, st);
+        case 4: return so ? hsum_tile_tz<4, true>(a, tz, grid, smem, st) : hsum_tile_tz<4, false>(a, tz, grid, smem, st);
+        case 8: return so ? hsum_tile_tz<8, true>(a, tz, grid, smem, st) : hsum_tile_tz<8, false>(a, tz, grid, smem, st);
+        case 16: return so ? hsum_tile_tz<16, true>(a, tz, grid, smem, st) : hsum_tile_tz<16, false>(a, tz, grid, smem, st);
     }
     return -1;
 }

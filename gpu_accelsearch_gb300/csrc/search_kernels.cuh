@@ -352,25 +352,26 @@ __host__ __device__ constexpr int stage_after(int h) {
     return ((h + 1) & h) ? -1 : (h == 0 ? 0 : h == 1 ? 1 : h == 3 ? 2 : h == 7 ? 3 : 4);
 }
 
-// Static shared memory of one harmonic-sum tile.
-template <int NH> struct TileShared {
-    int row[NH][kTileZ];  // byte offset of the row used by tile row zr
+// Static shared memory of one harmonic-sum tile of TZ f-dot rows.
+template <int NH, int TZ = kTileZ> struct TileShared {
+    int row[NH][TZ];      // byte offset of the row used by tile row zr
     int zf[NH], nzr[NH], r0[NH], c0[NH], w4[NH], off[NH];
     int cb[NH], crem[NH];  // column of tile column 0, and the rounding remainder
 };
 
-// One tile: segment seg, f-dot rows [z0, z0 + kTileZ), columns [i0, i0 +
+// One tile: segment seg, f-dot rows [z0, z0 + TZ), columns [i0, i0 +
 // kTileI), by the CTA's kTileI threads.  The CTA's mbarrier `bar` is
 // initialised here when init is set (its first use), else reused: the
 // caller passes the parity of this use.  Returns false -- with the error
 // word set -- when the copies did not land within the bounded wait; the
 // barrier's state is then unknown and the CTA must not use it again.
-template <int NH, bool STAGE_OUT>
+template <int NH, bool STAGE_OUT, int TZ = kTileZ>
 __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z0, int i0, float* tsm,
-                                               TileShared<NH>& S, unsigned long long* bar, bool init,
+                                               TileShared<NH, TZ>& S, unsigned long long* bar, bool init,
                                                unsigned parity) {
     static_assert(NH <= 32, "one lane per harmonic");
-    const int nz = min(kTileZ, a.numzs0 - z0);
+    static_assert(TZ % 4 == 0 && TZ <= kTileI, "rows in batches of four, one thread per row table entry");
+    const int nz = min(TZ, a.numzs0 - z0);
     const int ni = min(kTileI, a.uselen - i0);
     const long long startr = a.segs[seg].startr;
     const float* __restrict__ P = a.planes + (long long)seg * a.pstride;
@@ -449,7 +450,7 @@ __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z
     //    (rows past the plane's edge point at the rectangle's first row)
 #pragma unroll
     for (int h = 0; h < NH; h++) {
-        if (tid < kTileZ) {
+        if (tid < TZ) {
             const int r = (tid >= nz) ? 0 : (h == 0) ? tid : sub_row(a.zlo0 + kDz * (z0 + tid), a.h[h]) - S.zf[h];
             S.row[h][tid] = 4 * (S.off[h] + 4 * S.w4[h] * r);
         }
@@ -535,13 +536,13 @@ __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z
     return true;
 }
 
-template <int NH, bool STAGE_OUT>
-__global__ void __launch_bounds__(kTileI, 4) k_hsum_tile(const HsumArgs a) {
+template <int NH, bool STAGE_OUT, int TZ = kTileZ>
+__global__ void __launch_bounds__(kTileI, TZ > 16 ? 2 : 4) k_hsum_tile(const HsumArgs a) {
     extern __shared__ __align__(128) float tsm[];
-    __shared__ __align__(16) TileShared<NH> S;
+    __shared__ __align__(16) TileShared<NH, TZ> S;
     __shared__ __align__(8) unsigned long long s_bar;
-    hsum_tile_body<NH, STAGE_OUT>(a, blockIdx.z, blockIdx.y * kTileZ, blockIdx.x * kTileI, tsm, S, &s_bar, true,
-                                  0u);
+    hsum_tile_body<NH, STAGE_OUT, TZ>(a, blockIdx.z, blockIdx.y * TZ, blockIdx.x * kTileI, tsm, S, &s_bar, true,
+                                      0u);
 }
 
 // ------------------------------------------------------- pipelined tiled hsum

@@ -1,6 +1,6 @@
 // tune.cu -- the autotuner: picks the segment length and the launch shape
-// (launch-group size, plane-kernel thread layout) of a search by timing
-// them on the GPU it will run on.
+// (launch-group size, plane-kernel thread layout, harmonic-sum tile
+// height) of a search by timing them on the GPU it will run on.
 //
 // For every candidate segment length it builds a context, whitens a seeded
 // Gaussian spectrum generated on the device, and times accel_search_spectra
@@ -79,6 +79,33 @@ extern "C" int accel_autotune(const accel_config* base, const int* fftlens, int 
         rc = launch_noise_spectrum(spec, numbins, 0x5eedULL + li, st) ? ACCEL_ERR_CUDA : ACCEL_OK;
         if (!rc) rc = accel_whiten(ctx, reinterpret_cast<accel_complex*>(spec), numbins);
         const accel_complex* sp = reinterpret_cast<const accel_complex*>(spec);
+        long long nsteps = 0;
+        for (long long r = rlo; r + U / 2 < numbins; r += U / 2) nsteps++;
+        accel_harmonic h0;
+        accel_harmonic_info(ctx, 0, &h0);
+        // best of two timed searches (after a warm one), in cells per second
+        auto timed = [&](const accel_tuning& t, double* rate) -> int {
+            int r = accel_set_tuning(ctx, &t);
+            long long nc = 0;
+            if (!r) r = accel_search_spectra(ctx, 1, &sp, &numbins, &rlo, &nc);  // warm
+            if (r == ACCEL_ERR_CAPACITY) r = ACCEL_OK;
+            if (r) return r;
+            float best_ms = 1e30f;
+            for (int rep = 0; rep < 2; rep++) {
+                cudaEventRecord(t0, st);
+                r = accel_search_spectra(ctx, 1, &sp, &numbins, &rlo, &nc);
+                if (r == ACCEL_ERR_CAPACITY) r = ACCEL_OK;
+                cudaEventRecord(t1, st);
+                cudaEventSynchronize(t1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, t0, t1);
+                if (ms < best_ms) best_ms = ms;
+            }
+            *rate = (double)nsteps * U * h0.numzs / (best_ms * 1e-3);
+            return r;
+        };
+        const double best_before = best;
+        accel_tuning best_here{};
         for (int combo = 0; combo < 4 && !rc; combo++) {
             for (int ci = 0; ci < kChunks && !rc; ci++) {
                 if (ci > 0 && chunks[ci] > steps) break;  // the sample would fit in one group anyway
@@ -86,32 +113,29 @@ extern "C" int accel_autotune(const accel_config* base, const int* fftlens, int 
                 t.chunk_segments = chunks[ci];
                 t.plane_split = combo & 1;
                 t.fused_sum = combo >> 1;
-                rc = accel_set_tuning(ctx, &t);
-                long long nc = 0;
-                if (!rc) rc = accel_search_spectra(ctx, 1, &sp, &numbins, &rlo, &nc);  // warm
-                if (rc == ACCEL_ERR_CAPACITY) rc = ACCEL_OK;
+                double rate = 0.0;
+                rc = timed(t, &rate);
                 if (rc) break;
-                float best_ms = 1e30f;
-                for (int rep = 0; rep < 2; rep++) {
-                    cudaEventRecord(t0, st);
-                    rc = accel_search_spectra(ctx, 1, &sp, &numbins, &rlo, &nc);
-                    if (rc == ACCEL_ERR_CAPACITY) rc = ACCEL_OK;
-                    cudaEventRecord(t1, st);
-                    cudaEventSynchronize(t1);
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, t0, t1);
-                    if (ms < best_ms) best_ms = ms;
-                }
-                if (rc) break;
-                accel_harmonic h0;
-                accel_harmonic_info(ctx, 0, &h0);
-                long long nsteps = 0;
-                for (long long r = rlo; r + U / 2 < numbins; r += U / 2) nsteps++;
-                double rate = (double)nsteps * U * h0.numzs / (best_ms * 1e-3);
                 if (rate > best) {
                     best = rate;
                     *best_cfg = cfg;
                     best_cfg->chunk_segments = chunks[ci];
+                    *best_tuning = t;
+                    best_here = t;
+                }
+            }
+        }
+        // the tile height of the tiled harmonic sum, at the best shape of
+        // this segment length when it is the best so far
+        if (!rc && best > best_before && !best_here.fused_sum) {
+            for (int tz : {8, 32}) {
+                accel_tuning t = best_here;
+                t.hsum_tile_rows = tz;
+                double rate = 0.0;
+                rc = timed(t, &rate);
+                if (rc) break;
+                if (rate > best) {
+                    best = rate;
                     *best_tuning = t;
                 }
             }

@@ -114,7 +114,7 @@ def autotune(zmax=200, numharm=8, fftlens=(4096, 8192, 16384), steps=64, templat
     kw = dict(zmax=zmax, numharm=numharm, fftlen=best.fftlen, template_fp16=template_fp16,
               chunk_segments=best.chunk_segments, device=device)
     return kw, {"chunk_segments": tun.chunk_segments, "plane_split": tun.plane_split,
-                "fused_sum": tun.fused_sum}, rate.value
+                "fused_sum": tun.fused_sum, "hsum_tile_rows": tun.hsum_tile_rows or 16}, rate.value
 
 
 class AccelSearch:
@@ -198,11 +198,11 @@ class AccelSearch:
                 "fused_sum": t.fused_sum,
                 "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum,
                 "hsum_pipelined": t.hsum_pipelined, "graph": t.graph, "wait_test": t.wait_test,
-                "persistent": t.persistent}
+                "persistent": t.persistent, "hsum_tile_rows": t.hsum_tile_rows}
 
     def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
                    hsum_rowwise=None, serial_sum=None, hsum_pipelined=None, graph=None,
-                   wait_test=None, persistent=None):
+                   wait_test=None, persistent=None, hsum_tile_rows=None):
         cur = self.tuning()
         t = N.Tuning()
         t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
@@ -214,6 +214,7 @@ class AccelSearch:
         t.graph = cur["graph"] if graph is None else int(graph)
         t.wait_test = cur["wait_test"] if wait_test is None else int(wait_test)
         t.persistent = cur["persistent"] if persistent is None else int(persistent)
+        t.hsum_tile_rows = cur["hsum_tile_rows"] if hsum_tile_rows is None else int(hsum_tile_rows)
         N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
 
     def profile(self, enable: bool = True):

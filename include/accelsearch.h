@@ -117,6 +117,8 @@ typedef struct accel_tuning {
                             /* sequence keeps its shape); 0: direct launches. */
                             /* Searches that copy series from host memory     */
                             /* always launch directly                         */
+    int hsum_tile_rows;     /* f-dot rows per tile of the tiled harmonic sum: */
+                            /* 8, 16 (default; 0 reads as 16) or 32           */
     int persistent;         /* 1: a launch group's plane rows and harmonic-sum */
                             /* tiles run in one persistent launch from one    */
                             /* work queue, each segment summed as soon as its */

@@ -24,6 +24,7 @@ def test_autotuned_configuration_searches_like_the_hand_set_one():
     assert kw["fftlen"] in lens and rate > 0
     assert tun["chunk_segments"] in (16, 32, 64, 128, 256, 512)
     assert tun["plane_split"] in (0, 1) and tun["fused_sum"] in (0, 1)
+    assert tun["hsum_tile_rows"] in (8, 16, 32)
     n = 1 << 18
     x = synth_series(n, seed=77, signals=[(0.05, 30000.25, -24.0)])
     spec = np.fft.rfft(x.astype(np.float64)).astype(np.complex64)[: n // 2]
@@ -40,7 +41,7 @@ def test_autotuned_configuration_searches_like_the_hand_set_one():
         nsteps = s.step_count(n, DT)
     with AccelSearch(zmax=50, numharm=4, fftlen=kw["fftlen"], chunk_segments=tun["chunk_segments"]) as s:
         s.set_tuning(chunk_segments=tun["chunk_segments"], plane_split=tun["plane_split"],
-                     fused_sum=tun["fused_sum"])
+                     fused_sum=tun["fused_sum"], hsum_tile_rows=tun["hsum_tile_rows"])
         s.search_spectra([d.data_ptr()], [w.size], [rlo])
         by_hand = s.candidates()
     with AccelSearch(zmax=50, numharm=4, fftlen=kw["fftlen"]) as s:

@@ -242,10 +242,12 @@ def test_batched_equals_single(S, trial):
                           np.sort(both, order=["trial", "step", "numharm", "z", "r"]))
 
 
-@pytest.mark.parametrize("split,fused,chunk,serial,rowwise,pipelined",
-                         [(0, 1, 7, 0, 0, 0), (1, 1, 64, 1, 0, 0), (0, 0, 64, 1, 0, 1), (1, 0, 1, 0, 0, 0),
-                          (0, 0, 33, 0, 1, 0), (1, 0, 5, 0, 0, 1), (0, 0, 2, 0, 0, 0), (0, 0, 3, 1, 0, 0)])
-def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwise, pipelined):
+@pytest.mark.parametrize("split,fused,chunk,serial,rowwise,pipelined,rows",
+                         [(0, 1, 7, 0, 0, 0, 16), (1, 1, 64, 1, 0, 0, 16), (0, 0, 64, 1, 0, 1, 16),
+                          (1, 0, 1, 0, 0, 0, 16), (0, 0, 33, 0, 1, 0, 16), (1, 0, 5, 0, 0, 1, 16),
+                          (0, 0, 2, 0, 0, 0, 8), (0, 0, 3, 1, 0, 0, 32), (0, 0, 64, 0, 0, 0, 8),
+                          (0, 0, 64, 0, 0, 0, 32)])
+def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwise, pipelined, rows):
     # every launch shape gives bit-identical candidates (same float operations)
     w, rlo = trial["w"], trial["rlo"]
     d = dev(w)
@@ -256,12 +258,13 @@ def test_kernel_variants_identical(S, trial, split, fused, chunk, serial, rowwis
         S.search_spectra([d.data_ptr()], [w.size], [rlo])
         base = S.candidates()
         S.set_tuning(chunk_segments=chunk, plane_split=split, fused_sum=fused,
-                     serial_sum=serial, hsum_rowwise=rowwise, hsum_pipelined=pipelined)
+                     serial_sum=serial, hsum_rowwise=rowwise, hsum_pipelined=pipelined,
+                     hsum_tile_rows=rows)
         S.search_spectra([d.data_ptr()], [w.size], [rlo])
         got = S.candidates()
     finally:
         S.set_tuning(chunk_segments=64, plane_split=0, fused_sum=0, serial_sum=1,
-                     hsum_rowwise=0, hsum_pipelined=0)
+                     hsum_rowwise=0, hsum_pipelined=0, hsum_tile_rows=16)
         S.set_power_cuts([O.power_cut(6.0, 1 << s) for s in range(S.nstages)])
     assert len(base) > 10000
     assert np.array_equal(base, got)

@@ -4,7 +4,8 @@ kernel, k_step) against the separate kernels, through the C ABI: the same
 float operations in the same order, so the candidate sets must be
 bit-identical -- at ~3.5 sigma cuts (thousands of candidates), over launch
 groups of 1 to 64 segments, FP32 and FP16 templates, graph and direct
-launches, and a batch of uneven trials.  Its bounded waits are tested
+launches, and a batch of uneven trials.  The separate tiled sum at tile
+heights of 8 and 32 rows gives the same candidates too.  Its bounded waits are tested
 without a GPU fault: with tuning.wait_test every tile's copy wait runs out,
 the search fails with ACCEL_ERR_CUDA and the context recovers."""
 import numpy as np
@@ -47,6 +48,11 @@ def test_persistent_equals_separate_kernels(zmax, numharm):
                 continue
             assert nstep > 0, chunk
             assert np.array_equal(got, base), chunk
+        # and the separate tiled sum at its other tile heights
+        for rows in (8, 32):
+            got, _ = search(s, d, w.size, 16, chunk_segments=16, persistent=0, hsum_tile_rows=rows)
+            assert np.array_equal(got, base), rows
+        s.set_tuning(hsum_tile_rows=16)
 
 
 def test_persistent_fp16_graph_direct_and_batches():
