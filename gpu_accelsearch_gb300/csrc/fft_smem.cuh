@@ -4,10 +4,14 @@
 // thread t is point t + e*T both on entry (time order) and on exit
 // (frequency order), so loads from and stores to global memory coalesce.
 // Between passes the points go through shared memory (one element of
-// padding every 16 keeps the stride-16 stores free of bank conflicts).
+// padding every 16 keeps the stride-16 stores free of bank conflicts; the
+// padding of every offset that is a multiple of 16 is a constant, so each
+// access costs one base index per pass and an immediate offset).
 //
 // NB independent transforms of the same length are done side by side by
-// the same threads (one barrier per pass for all of them).
+// the same threads (one barrier per pass for all of them), each through its
+// own padded buffer: a transform's butterflies run while the other's
+// shared-memory stores and loads are still in flight.
 //
 // Twiddles come from a table tw[m] = exp(+2 pi i m / kTwN) in global
 // memory (computed once from double precision); the forward direction uses
@@ -84,11 +88,21 @@ template <int DIR> __device__ __forceinline__ void dft8(float2* v) {
     }
 }
 
+__device__ __forceinline__ float2 cfma(float s, float2 a, float2 b) {  // s a + b
+    return make_float2(fmaf(s, a.x, b.x), fmaf(s, a.y, b.y));
+}
+
 // 16 points as 4 x 4: x[4 n1 + n2] -> X[k1 + 4 k2].  DFT4 over n1 for each
-// n2, twiddles W16^(n2 k1), DFT4 over n2 for each k1 (148 real operations
-// instead of 168 for the 2 x 8 split).
+// n2, twiddles W16^(n2 k1), DFT4 over n2 for each k1.  Each nontrivial
+// twiddle is written as a real scale times a factor with a unit component
+// -- W^2 = s (1 + i'), W^6 = s (-1 + i'), W^1 = c (1 + t i'), W^3 =
+// c (t + i'), W^9 = -c (1 + t i') with i' = DIR i, s = 1/sqrt2,
+// c = cos(pi/8), t = tan(pi/8) -- and the scale is applied by the fused
+// multiply-adds of the second DFT4 layer, whose two inputs of a pair carry
+// the same scale: 144 floating-point instructions per 16 points instead of
+// 160 with the twiddles multiplied out.
 template <int DIR> __device__ __forceinline__ void dft16(float2* v) {
-    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+    const float C = 0.92387953251128675613f, S = 0.70710678118654752440f, TN = 0.41421356237309504880f;
     float2 y[4][4];  // y[n2][k1]
 #pragma unroll
     for (int n2 = 0; n2 < 4; n2++) {
@@ -97,22 +111,36 @@ template <int DIR> __device__ __forceinline__ void dft16(float2* v) {
 #pragma unroll
         for (int k1 = 0; k1 < 4; k1++) y[n2][k1] = u[k1];
     }
-    // W16^1, W16^2, W16^3 | W16^2, W16^4, W16^6 | W16^3, W16^6, W16^9 = -W16^1
-    y[1][1] = cmul(y[1][1], make_float2(c1, DIR * s1));
-    y[1][2] = w8_1<DIR>(y[1][2]);
-    y[1][3] = cmul(y[1][3], make_float2(s1, DIR * c1));
-    y[2][1] = w8_1<DIR>(y[2][1]);
-    y[2][2] = mul_i<DIR>(y[2][2]);
-    y[2][3] = w8_3<DIR>(y[2][3]);
-    y[3][1] = cmul(y[3][1], make_float2(s1, DIR * c1));
-    y[3][2] = w8_3<DIR>(y[3][2]);
-    y[3][3] = cmul(y[3][3], make_float2(-c1, -DIR * s1));
-#pragma unroll
-    for (int k1 = 0; k1 < 4; k1++) {
-        float2 u[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    {  // k1 = 0: no twiddles
+        float2 u[4] = {y[0][0], y[1][0], y[2][0], y[3][0]};
         dft4<DIR>(u);
-#pragma unroll
-        for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = u[k2];
+        v[0] = u[0], v[4] = u[1], v[8] = u[2], v[12] = u[3];
+    }
+    {  // k1 = 1: W^1 = c (1 + t i'), W^2 = s (1 + i'), W^3 = c (t + i')
+        const float2 p2 = cadd(y[2][1], mul_i<DIR>(y[2][1]));
+        const float2 s02 = cfma(S, p2, y[0][1]), d02 = cfma(-S, p2, y[0][1]);
+        const float2 i1 = mul_i<DIR>(y[1][1]), i3 = mul_i<DIR>(y[3][1]);
+        const float2 a1 = cfma(TN, i1, y[1][1]), a3 = cfma(TN, y[3][1], i3);
+        const float2 s13 = cadd(a1, a3), d13 = mul_i<DIR>(csub(a1, a3));
+        v[1] = cfma(C, s13, s02), v[9] = cfma(-C, s13, s02);
+        v[5] = cfma(C, d13, d02), v[13] = cfma(-C, d13, d02);
+    }
+    {  // k1 = 2: W^2 = s (1 + i'), W^4 = i', W^6 = s (-1 + i')
+        const float2 i2 = mul_i<DIR>(y[2][2]);
+        const float2 s02 = cadd(y[0][2], i2), d02 = csub(y[0][2], i2);
+        const float2 a = csub(y[1][2], y[3][2]), ib = mul_i<DIR>(cadd(y[1][2], y[3][2]));
+        const float2 s13 = cadd(a, ib), d13 = csub(ib, a);
+        v[2] = cfma(S, s13, s02), v[10] = cfma(-S, s13, s02);
+        v[6] = cfma(S, d13, d02), v[14] = cfma(-S, d13, d02);
+    }
+    {  // k1 = 3: W^3 = c (t + i'), W^6 = s (-1 + i'), W^9 = -c (1 + t i')
+        const float2 p2 = csub(mul_i<DIR>(y[2][3]), y[2][3]);
+        const float2 s02 = cfma(S, p2, y[0][3]), d02 = cfma(-S, p2, y[0][3]);
+        const float2 i1 = mul_i<DIR>(y[1][3]), i3 = mul_i<DIR>(y[3][3]);
+        const float2 a1 = cfma(TN, y[1][3], i1), a3 = cfma(TN, i3, y[3][3]);
+        const float2 s13 = csub(a1, a3), d13 = mul_i<DIR>(cadd(a1, a3));
+        v[3] = cfma(C, s13, s02), v[11] = cfma(-C, s13, s02);
+        v[7] = cfma(C, d13, d02), v[15] = cfma(-C, d13, d02);
     }
 }
 
@@ -216,6 +244,17 @@ __device__ __forceinline__ void apply_tw16(float2 (&v)[NB][16], const Tw16& p) {
         for (int r = 1; r < 16; r++) v[nb][r] = cmul(v[nb][r], w[r]);
 }
 
+// Padded shared-memory index of point t + q T + r M/R, the point a pass
+// loads into its register q + r Q: for M >= 256 the offset is a multiple of
+// 16, so its padding is a constant.
+template <int M, int R>
+__device__ __forceinline__ int fft_load_index(int tp, int t, int q, int r) {
+    constexpr int T = M / 16;
+    const int o = q * T + r * (M / R);
+    if constexpr (T % 16 == 0 && (M / R) % 16 == 0) return tp + o + (o >> 4);
+    else return fft_pad(t + o);
+}
+
 // One Stockham pass of radix R over NB transforms.  FIRST: input already in
 // registers (time order).  LAST: output left in registers (frequency order).
 // PRE: twiddles of a radix-16 pass supplied by the caller (Q == 1).
@@ -226,27 +265,17 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
     constexpr int T = M / 16;
     constexpr int Q = 16 / R;
     constexpr int PM = FftShape<M>::PADDED;
+    // the stores of a pass go to j + r NS with j a multiple of 16 (first
+    // pass) or NS a multiple of 16: constant padding again
+    static_assert(LAST || (NS == 1 && R == 16) || NS % 16 == 0, "store offsets must pad by a constant");
     if constexpr (!FIRST) {
-        if constexpr (NB == 2) {
-            // both transforms' values of one index side by side: one 16-byte access
-            const float4* sm4 = reinterpret_cast<const float4*>(sm);
+        const int tp = fft_pad(t);
+#pragma unroll
+        for (int nb = 0; nb < NB; nb++)
 #pragma unroll
             for (int q = 0; q < Q; q++)
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    const float4 v = sm4[fft_pad(t + q * T + r * (M / R))];
-                    a[0][q + r * Q] = make_float2(v.x, v.y);
-                    a[1][q + r * Q] = make_float2(v.z, v.w);
-                }
-        } else {
-#pragma unroll
-            for (int nb = 0; nb < NB; nb++)
-#pragma unroll
-                for (int q = 0; q < Q; q++)
-#pragma unroll
-                    for (int r = 0; r < R; r++)
-                        a[nb][q + r * Q] = sm[nb * PM + fft_pad(t + q * T + r * (M / R))];
-        }
+                for (int r = 0; r < R; r++) a[nb][q + r * Q] = sm[nb * PM + fft_load_index<M, R>(tp, t, q, r)];
         sync();
     }
 #pragma unroll
@@ -269,25 +298,14 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
                 apply_twiddles<R, DIR, NB>(v, tw, k, NS * R);
             }
         }
+        const int jp = fft_pad((b / NS) * (NS * R) + k);
 #pragma unroll
-        for (int nb = 0; nb < NB; nb++) dft<R, DIR>(v[nb]);
-        if constexpr (LAST) {
+        for (int nb = 0; nb < NB; nb++) {
+            dft<R, DIR>(v[nb]);
 #pragma unroll
-            for (int nb = 0; nb < NB; nb++)
-#pragma unroll
-                for (int r = 0; r < R; r++) a[nb][q + r * Q] = v[nb][r];
-        } else {
-            const int j = (b / NS) * (NS * R) + k;
-            if constexpr (NB == 2) {
-                float4* sm4 = reinterpret_cast<float4*>(sm);
-#pragma unroll
-                for (int r = 0; r < R; r++)
-                    sm4[fft_pad(j + r * NS)] = make_float4(v[0][r].x, v[0][r].y, v[1][r].x, v[1][r].y);
-            } else {
-#pragma unroll
-                for (int nb = 0; nb < NB; nb++)
-#pragma unroll
-                    for (int r = 0; r < R; r++) sm[nb * PM + fft_pad(j + r * NS)] = v[nb][r];
+            for (int r = 0; r < R; r++) {
+                if constexpr (LAST) a[nb][q + r * Q] = v[nb][r];
+                else sm[nb * PM + jp + r * NS + ((r * NS) >> 4)] = v[nb][r];
             }
         }
     }
@@ -297,8 +315,7 @@ __device__ __forceinline__ void fft_pass(float2 (&a)[NB][16], float2* sm,
 // Full transform: radix-16 passes, the leftover factor (2, 4 or 8) last.
 // t is the thread's index within the group of M/16 threads doing the
 // transform(s); sm (16-byte aligned) must hold NB * FftShape<M>::PADDED
-// float2 -- for two transforms as PADDED float4, both transforms' values
-// of an index side by side.  The twiddles of the radix-16 passes after the
+// float2, one padded buffer per transform.  The twiddles of the radix-16 passes after the
 // first are loaded up front.  Shared memory may be rewritten as soon as
 // this returns.
 template <int M, int DIR, int NB, class Sync = CtaSync>

@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(PlaneShape<SPLIT, M>::THREADS, PlaneShape<SPLI
         plane_powers<M, F16, false>(H, D, z, reinterpret_cast<float2*>(smem_raw), tw, p, t);
 #pragma unroll
         for (int e = 0; e < 16; e++) {
-            const int i2 = t + e * T - H.hw0;
-            if (i2 >= 0 && i2 < half_w) *reinterpret_cast<float2*>(row + 2 * i2) = p[e];
+            const int i2 = t + e * T - H.hw0;  // one unsigned compare for 0 <= i2 < half_w
+            if ((unsigned)i2 < (unsigned)half_w) *reinterpret_cast<float2*>(row + 2 * i2) = p[e];
         }
     } else {
         // even transform, then odd, each stored as it completes (a loop, not
