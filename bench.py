@@ -64,6 +64,10 @@ def parse():
                     help="seeds of the FP16-template precision report (0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=5.0,
                     help="duration of the Poisson arrival process of the serving leg (0: skip)")
+    ap.add_argument("--serving-chunk", type=int, default=128, help="segments per launch group of the server")
+    ap.add_argument("--serving-lengths", default="log-uniform", choices=["log-uniform", "octaves"],
+                    help="request lengths: log-uniform 2^18..2^23 (every request a new length), or "
+                         "rounded down to powers of two")
     return ap.parse_args()
 
 
@@ -157,7 +161,7 @@ def smooth_length(n: int) -> int:
             return m
         m += 2
 
-def run_serving(seconds: float, device: int, rate: float = 200.0):
+def run_serving(seconds: float, device: int, rate: float = 200.0, chunk: int = 128, lengths: str = "log-uniform"):
     """The serving configuration: Poisson arrivals at `rate` per second of
     DM-trial series with lengths log-uniform in 2^18..2^23 samples, zmax
     uniform in {50, 100, 200, 300}, 5% with an injected signal, admitted
@@ -176,10 +180,12 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
         if t > seconds:
             break
         n = smooth_length(int(2 ** rng.uniform(18, 23)))
+        if lengths == "octaves":  # a few fixed lengths: one R2C plan each
+            n = 1 << int(np.floor(np.log2(n)))
         zmax = int(rng.choice([50, 100, 200, 300]))
         src = sig[rng.integers(len(sig))] if rng.random() < 0.05 else pool[rng.integers(len(pool))]
         arrivals.append((t, src[:n], zmax))
-    srv = Server(hbm_budget_bytes=150e9, fftlen=8192, numharm=8, chunk_segments=128, device=device)
+    srv = Server(hbm_budget_bytes=150e9, fftlen=8192, numharm=8, chunk_segments=chunk, device=device)
     for z in (50, 100, 200, 300):  # build the four banks outside the measurement
         srv.wait(srv.submit(pool[0][: 1 << 18], DT, z), -1)
     base = srv.stats()
@@ -190,19 +196,26 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
         if dly > 0:
             time.sleep(dly)
         ids.append(srv.submit(x, DT, z))
-    lats = []
+    lats, parts = [], []
     for rid in ids:
         srv.wait(rid, -1)
         lats.append(srv.result(rid)[1])
     wall = time.perf_counter() - t0
-    # latency by length class (octaves of the sample count)
+    for rid in ids:
+        parts.append(srv.timing(rid))
+    # latency by length class (octaves of the sample count), with the median
+    # of each part of it
     by_class = {}
-    for (ta, x, z), lat in zip(arrivals, lats):
+    for (ta, x, z), lat, pt in zip(arrivals, lats, parts):
         k = int(np.floor(np.log2(x.size)))
-        by_class.setdefault(k, []).append(lat)
-    classes = {f"2^{k}..2^{k + 1}": {"requests": len(v), "p50_ms": float(np.percentile(v, 50)),
-                                      "p99_ms": float(np.percentile(v, 99))}
-               for k, v in sorted(by_class.items())}
+        by_class.setdefault(k, []).append((lat, pt))
+    classes = {}
+    for k, v in sorted(by_class.items()):
+        lv = [a for a, _ in v]
+        classes[f"2^{k}..2^{k + 1}"] = dict(
+            {"requests": len(v), "p50_ms": float(np.percentile(lv, 50)), "p99_ms": float(np.percentile(lv, 99))},
+            **{"median_" + key: float(np.median([p[key] for _, p in v]))
+               for key in ("queue_ms", "prepare_ms", "wait_ms", "search_ms")})
     st = srv.stats()
     srv.close()
     cells = st["cells"] - base["cells"]
@@ -214,7 +227,17 @@ def run_serving(seconds: float, device: int, rate: float = 200.0):
             "cells_per_s": cells / wall, "cells_per_gpu_s": cells / gpu_s if gpu_s else None,
             "admission_thread_s": (st["admit_ms"] - base["admit_ms"]) / 1e3,
             "scheduler_group_s": (st["group_ms"] - base["group_ms"]) / 1e3,
-            "wall_s": wall, "hbm_budget_bytes": 150e9, "max_wait_s": 1.0, "by_length": classes,
+            "gpu_search_s": gpu_s,
+            "gpu_gap_s": (st["gap_ms"] - base["gap_ms"]) / 1e3,
+            "gpu_idle_s": (st["idle_ms"] - base["idle_ms"]) / 1e3,
+            "scheduler_wait_s": (st["wait_ms"] - base["wait_ms"]) / 1e3,
+            "scheduler_launch_s": (st["launch_ms"] - base["launch_ms"]) / 1e3,
+            "gpu_prepare_s": (st["prep_gpu_ms"] - base["prep_gpu_ms"]) / 1e3,
+            "groups": st["groups"] - base["groups"],
+            "segments_per_group": (st["group_segments"] - base["group_segments"]) / max(1, st["groups"] - base["groups"]),
+            "wall_s": wall, "hbm_budget_bytes": 150e9, "max_wait_s": 1.0, "chunk_segments": chunk,
+            "lengths": lengths,
+            "by_length": classes,
             "workload": "Poisson arrivals, lengths log-uniform 2^18..2^23 (rounded up to even "
                         "7-smooth lengths), "
                         "zmax uniform in {50,100,200,300}, 5% with a signal, L=8192, 8 harmonics, "
@@ -693,9 +716,11 @@ def run_ours(args):
         finally:
             cpu.close()
     dedisp = run_dedisperse(local) if args.serving_seconds > 0 else None
-    serving = run_serving(args.serving_seconds, local) if args.serving_seconds > 0 else None
+    serving = (run_serving(args.serving_seconds, local, chunk=args.serving_chunk, lengths=args.serving_lengths)
+               if args.serving_seconds > 0 else None)
     # the same stream at half the rate: latency when the GPU is not saturated
-    serving_half = (run_serving(args.serving_seconds, local, rate=100.0)
+    serving_half = (run_serving(args.serving_seconds, local, rate=100.0, chunk=args.serving_chunk,
+                                lengths=args.serving_lengths)
                     if args.serving_seconds > 0 else None)
     precision = precision_report(args.precision_seeds, local) if args.precision_seeds > 0 else None
     line = {

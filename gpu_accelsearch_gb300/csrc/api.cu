@@ -433,34 +433,10 @@ int do_whiten(accel_ctx* c, float2* spec, unsigned numbins) {
 }
 
 int do_rfft(accel_ctx* c, const float* series, long long n, float2* spec) {
-    cufftHandle plan;
-    auto it = c->fftplans.find(n);
-    if (it == c->fftplans.end()) {
-        // bounded plan cache: drop the least recently used plan
-        if (c->fftplans.size() >= 64) {
-            auto lru = std::min_element(c->fftplan_use.begin(), c->fftplan_use.end(),
-                                        [](const std::pair<const long long, long long>& a,
-                                           const std::pair<const long long, long long>& b) {
-                                            return a.second < b.second;
-                                        });
-            CK(cudaStreamSynchronize(c->stream));
-            cufftDestroy(c->fftplans[lru->first]);
-            c->fftplans.erase(lru->first);
-            c->fftplan_use.erase(lru);
-        }
-        if (cufftPlan1d(&plan, (int)n, CUFFT_R2C, 1) != CUFFT_SUCCESS)
-            return set_err(ACCEL_ERR_CUDA, "cufftPlan1d(%lld, R2C) failed", n);
-        c->fftplans[n] = plan;
-    } else {
-        plan = it->second;
-    }
-    c->fftplan_use[n] = ++c->fftplan_clock;
     ProfScope ps(c, K_RFFT, 1);
-    if (cufftSetStream(plan, c->stream) != CUFFT_SUCCESS)
-        return set_err(ACCEL_ERR_CUDA, "cufftSetStream failed");
-    if (cufftExecR2C(plan, const_cast<float*>(series), reinterpret_cast<cufftComplex*>(spec)) !=
-        CUFFT_SUCCESS)
-        return set_err(ACCEL_ERR_CUDA, "cufftExecR2C failed");
+    const int r = r2c_any(c->r2c, series, n, spec, c->stream);
+    if (r == -2) return set_err(ACCEL_ERR_NOMEM, "real-to-complex transform of %lld samples: scratch memory", n);
+    if (r) return set_err(ACCEL_ERR_CUDA, "real-to-complex transform of %lld samples failed", n);
     return ACCEL_OK;
 }
 
@@ -869,7 +845,8 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
 void free_ctx(accel_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    for (auto& kv : c->fftplans) cufftDestroy(kv.second);
+    for (auto& kv : c->r2c.plans) cufftDestroy(kv.second);
+    c->r2c.plans.clear();
     for (auto& e : c->pending) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);

@@ -23,6 +23,19 @@ struct WhitenPlanDev {
     long long last_use = 0;
 };
 
+// Real-to-complex transforms of any even length from power-of-two C2C
+// plans (rfft.cu).  One thread uses an engine at a time.
+struct R2CEngine {
+    std::map<long long, cufftHandle> plans;  // C2C plans by power-of-two length
+    R2CEngine() = default;
+    R2CEngine(const R2CEngine&) = delete;
+    R2CEngine& operator=(const R2CEngine&) = delete;
+    ~R2CEngine();
+};
+// spec[0 .. n/2] = the DFT of the n real samples of x (device, n even), on
+// stream st: 0, -1 on a CUDA or cuFFT error, -2 when scratch memory runs out.
+int r2c_any(R2CEngine& e, const float* x, long long n, float2* spec, cudaStream_t st);
+
 struct TrialBuf {
     long long n = 0;            // allocated samples
     long long numbins = 0;      // whitened bins of the last search
@@ -94,9 +107,7 @@ struct accel_ctx {
 
     std::map<unsigned, WhitenPlanDev> wplans;  // by spectrum length, at most kWhitenPlans
     long long wplan_clock = 0;
-    std::map<long long, cufftHandle> fftplans;
-    std::map<long long, long long> fftplan_use;  // last use of each plan (LRU)
-    long long fftplan_clock = 0;
+    R2CEngine r2c;  // the trials' real-to-complex transforms
     std::vector<TrialBuf> trials;
 
     std::vector<accel_candidate> results;

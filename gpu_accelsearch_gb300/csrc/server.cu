@@ -1,13 +1,11 @@
 // server.cu -- continuous-batching request server (accel_server_*).
 //
 // Requests are single DM-trial time series.
-//   * An admission thread admits queued requests in arrival order, as their
-//     R2C plans are ready, while their device memory (series + spectrum)
-//     fits the HBM budget and the active limit: it copies the series in and
-//     runs the R2C transform and whitening on its own stream, records an
-//     event and hands the request to the scheduler.  (Copies from pageable
-//     host memory block the calling thread; on their own thread they no
-//     longer hold up the launches.)
+//   * An admission thread admits queued requests in arrival order while
+//     their device memory (series + spectrum) fits the HBM budget and the
+//     active limit: it copies the series in through pinned staging buffers
+//     and runs the R2C transform and whitening on its own stream, records
+//     an event and hands the request to the scheduler.
 //   * The scheduler thread orders its stream after each handed-over
 //     request's event and builds each launch group from the active requests
 //     of one template bank (one bank per zmax, created on first use),
@@ -29,13 +27,12 @@
 // Each segment is computed independently of the others in its group, so a
 // request's result does not depend on what it was batched with.
 //
-// Planner threads make each request's cuFFT R2C plan when the request is
-// submitted (making a plan for a new length costs about 2 ms of host time,
-// and almost every request of a serving stream has a new length), without
-// work area: the worker runs every transform on one stream with one shared
-// work area.  A queued request is admitted once its plan is ready.  Plans
-// no queued or active request needs are destroyed once more than
-// kPlanCache of them exist.
+// Almost every request of a serving stream has a length of its own.  The
+// R2C transform therefore runs on power-of-two cuFFT plans only (rfft.cu):
+// making a cuFFT plan per length took 6-19 ms of host time per request on
+// the planner threads of an earlier design and, while it ran, held up every
+// CUDA call of the scheduler (kernel launches 0.5 ms instead of 18 us per
+// launch group), leaving the GPU waiting between groups.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -44,7 +41,6 @@
 #include <map>
 #include <memory>
 #include <mutex>
-#include <set>
 #include <thread>
 #include <vector>
 
@@ -69,17 +65,26 @@ struct Request {
     float2* d_spec = nullptr;
     double bytes = 0;
     int state = 0;  // 0 queued, 1 active, 2 done, 3 failed
+    bool prepared = false;  // its ready event has completed (seen from the host)
     int rc = ACCEL_OK;
     cudaEvent_t ready = nullptr;  // end of its copy, R2C and whitening (admission stream)
+    cudaEvent_t ev_prep = nullptr;  // start of its R2C (after the copy): GPU time of the preparation
     std::vector<accel_candidate> cands;
-    Clock::time_point t_submit, t_done;
+    // submission, admission start, admission's host work done, first launch
+    // group issued, completion (accel_server_timing)
+    Clock::time_point t_submit, t_admit, t_prepared, t_first, t_done;
 };
+
+// Candidates read back with a launch group's count (pinned, asynchronous);
+// a group with more reads the rest afterwards.
+constexpr int kCandStage = 8192;
 
 // Device and pinned host buffers of one launch group in flight.
 struct GroupBuf {
     SegDesc* d_segs = nullptr;
     SegDesc* h_segs = nullptr;                // pinned
     RawCand* d_cands = nullptr;
+    RawCand* h_cands = nullptr;               // pinned, kCandStage
     unsigned long long* d_ncand = nullptr;    // count, error word
     unsigned long long* h_ncand = nullptr;    // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr; // the group's kernels
@@ -96,17 +101,15 @@ struct Group {
 // A launched group whose candidates have not been read yet.
 struct Flight {
     int zmax = -1, b = 0, n = 0, rc = ACCEL_OK;
+    bool after_idle = false;  // launched after every earlier group had been read back
     std::vector<std::pair<Request*, long long>> owner;  // per segment: request, step
 };
 
-struct R2CPlan {
-    cufftHandle plan = 0;
-    size_t work = 0;  // work-area bytes
-    bool ok = false;
-};
-
-constexpr size_t kPlanCache = 256;
-constexpr int kPlanners = 4;
+// Series reach the device through two pinned staging buffers: the
+// admission thread copies a chunk of the caller's (pageable) memory into one
+// with the CPU while the other's DMA runs.  (A copy straight from pageable
+// memory makes the driver stage it, holding up the scheduler's launches.)
+constexpr long long kStageFloats = 1LL << 22;  // 16 MB per buffer
 
 }  // namespace
 
@@ -114,7 +117,10 @@ struct accel_server {
     accel_server_config cfg{};
     cudaStream_t stream = nullptr;   // launch groups (scheduler thread)
     cudaStream_t astream = nullptr;  // copies, R2C and whitening (admission thread)
-    accel_ctx* wctx = nullptr;       // whitening plans of the admission thread
+    float* stage[2] = {nullptr, nullptr};            // pinned staging (admission thread)
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};    // each buffer's last DMA
+    bool stage_used[2] = {false, false};
+    accel_ctx* wctx = nullptr;       // R2C engine and whitening plans of the admission thread
     std::thread worker, admitter;
     bool admitter_done = false;
     std::deque<Request*> ready;      // admitted and prepared, not yet with the scheduler
@@ -125,21 +131,10 @@ struct accel_server {
     std::map<long long, std::unique_ptr<Request>> reqs;
     std::map<int, Group> groups;
     long long next_id = 1;
-    // R2C plans by series length (planner thread; guarded by plan_mu)
-    std::vector<std::thread> planners;    // kPlanners threads
-    std::mutex plan_mu;
-    std::condition_variable plan_cv;
-    bool plan_stop = false;
-    bool plan_evict = false;              // a cached plan lost its last user
-    std::deque<long long> plan_queue;
-    std::map<long long, R2CPlan> plans;
-    std::map<long long, int> plan_users;  // queued or active requests per length
-    std::set<long long> planning;         // lengths queued or being planned
-    void* work = nullptr;                 // shared cuFFT work area (worker thread)
-    size_t work_bytes = 0;
     double bytes_in_use = 0;
     accel_server_stats st{};
     std::deque<Flight> flights;  // launched groups not yet read back, oldest first
+    cudaEvent_t last_ev1 = nullptr;  // end of the last group read back (its buffer is not reused before the next read)
     bool late_turn = true;       // the next group serves the late requests (when there are any)
 };
 
@@ -147,27 +142,40 @@ namespace {
 
 double request_bytes(long long n) { return 4.0 * n + 8.0 * (n / 2 + 1); }
 
-void release_plan(accel_server* s, long long n) {
-    bool wake = false;
-    {
-        std::lock_guard<std::mutex> lk(s->plan_mu);
-        auto it = s->plan_users.find(n);
-        if (it != s->plan_users.end() && --it->second <= 0) {
-            s->plan_users.erase(it);
-            wake = s->plan_evict = s->plans.size() > kPlanCache;
+// Whether a request's copy, transform and whitening have finished on the
+// admission stream, seen from the host: a launch group takes a request only
+// then, so that the group stream never waits on the admission stream (for
+// a large request, milliseconds of copy and transform) before a group that
+// may not even hold it.  (An error there is sticky: the group that takes
+// the request reports it.)
+bool is_prepared(accel_server* s, Request* r) {
+    if (!r->prepared && cudaEventQuery(r->ready) != cudaErrorNotReady) {
+        r->prepared = true;
+        float ms = 0.f;
+        if (r->ev_prep && cudaEventElapsedTime(&ms, r->ev_prep, r->ready) == cudaSuccess) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->st.prep_gpu_ms += ms;
         }
     }
-    if (wake) s->plan_cv.notify_all();
+    return r->prepared;
+}
+
+Request* first_unprepared(accel_server* s) {
+    for (auto& kv : s->groups)
+        for (Request* r : kv.second.active)
+            if (r->next_step < r->nsteps && !r->prepared) return r;
+    return nullptr;
 }
 
 void finish(accel_server* s, Request* r, int rc, cudaStream_t st) {
     if (r->d_series) cudaFreeAsync(r->d_series, st);
     if (r->d_spec) cudaFreeAsync(r->d_spec, st);
     if (r->ready) cudaEventDestroy(r->ready);
+    if (r->ev_prep) cudaEventDestroy(r->ev_prep);
     r->ready = nullptr;
+    r->ev_prep = nullptr;
     r->d_series = nullptr;
     r->d_spec = nullptr;
-    release_plan(s, r->n);
     r->rc = rc;
     r->t_done = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
@@ -184,6 +192,7 @@ void free_group(Group& g) {
         cudaFree(b.d_segs);
         cudaFreeHost(b.h_segs);
         cudaFree(b.d_cands);
+        cudaFreeHost(b.h_cands);
         cudaFree(b.d_ncand);
         cudaFreeHost(b.h_ncand);
         if (b.ev0) cudaEventDestroy(b.ev0);
@@ -221,6 +230,7 @@ accel_ctx* group_ctx(accel_server* s, int zmax, int* rc) {
         if (cudaMalloc(&b.d_segs, sizeof(SegDesc) * cap) != cudaSuccess ||
             cudaMallocHost(&b.h_segs, sizeof(SegDesc) * cap) != cudaSuccess ||
             cudaMalloc(&b.d_cands, sizeof(RawCand) * g.ctx->cand_cap) != cudaSuccess ||
+            cudaMallocHost(&b.h_cands, sizeof(RawCand) * kCandStage) != cudaSuccess ||
             cudaMalloc(&b.d_ncand, 2 * sizeof(unsigned long long)) != cudaSuccess ||
             cudaMallocHost(&b.h_ncand, 2 * sizeof(unsigned long long)) != cudaSuccess ||
             cudaEventCreate(&b.ev0) != cudaSuccess || cudaEventCreate(&b.ev1) != cudaSuccess ||
@@ -241,33 +251,31 @@ int admit(accel_server* s, Request* r) {
     if (cudaMallocAsync(&r->d_series, sizeof(float) * r->n, s->astream) != cudaSuccess ||
         cudaMallocAsync(&r->d_spec, sizeof(float2) * (r->n / 2 + 1), s->astream) != cudaSuccess)
         return set_error(ACCEL_ERR_NOMEM, "request %lld: device allocation", r->id);
-    if (cudaMemcpyAsync(r->d_series, r->host, sizeof(float) * r->n, cudaMemcpyHostToDevice, s->astream) !=
-        cudaSuccess)
+    if (s->stage[0] && s->stage[1]) {
+        int k = 0;
+        for (long long off = 0; off < r->n; off += kStageFloats, k ^= 1) {
+            const long long m = std::min(kStageFloats, r->n - off);
+            if (s->stage_used[k] && cudaEventSynchronize(s->stage_ev[k]) != cudaSuccess)
+                return set_error(ACCEL_ERR_CUDA, "request %lld: staging", r->id);
+            std::memcpy(s->stage[k], r->host + off, sizeof(float) * m);
+            if (cudaMemcpyAsync(r->d_series + off, s->stage[k], sizeof(float) * m, cudaMemcpyHostToDevice,
+                                s->astream) != cudaSuccess ||
+                cudaEventRecord(s->stage_ev[k], s->astream) != cudaSuccess)
+                return set_error(ACCEL_ERR_CUDA, "request %lld: copy", r->id);
+            s->stage_used[k] = true;
+        }
+    } else if (cudaMemcpyAsync(r->d_series, r->host, sizeof(float) * r->n, cudaMemcpyHostToDevice, s->astream) !=
+               cudaSuccess) {
         return set_error(ACCEL_ERR_CUDA, "request %lld: copy", r->id);
-    R2CPlan pl;
-    {
-        std::unique_lock<std::mutex> lk(s->plan_mu);
-        s->plan_cv.wait(lk, [&] { return s->plans.count(r->n) != 0; });
-        pl = s->plans[r->n];
     }
-    if (!pl.ok) return set_error(ACCEL_ERR_CUDA, "request %lld: cuFFT plan for %lld samples", r->id, r->n);
-    if (pl.work > s->work_bytes) {
-        // grow the shared work area (transforms in flight use the old one)
-        if (cudaStreamSynchronize(s->astream) != cudaSuccess)
-            return set_error(ACCEL_ERR_CUDA, "request %lld: stream", r->id);
-        cudaFree(s->work);
-        s->work = nullptr;
-        s->work_bytes = 0;
-        if (cudaMalloc(&s->work, pl.work) != cudaSuccess)
-            return set_error(ACCEL_ERR_NOMEM, "request %lld: cuFFT work area", r->id);
-        s->work_bytes = pl.work;
-    }
-    if (cufftSetWorkArea(pl.plan, s->work) != CUFFT_SUCCESS || cufftSetStream(pl.plan, s->astream) != CUFFT_SUCCESS ||
-        cufftExecR2C(pl.plan, r->d_series, reinterpret_cast<cufftComplex*>(r->d_spec)) != CUFFT_SUCCESS)
-        return set_error(ACCEL_ERR_CUDA, "request %lld: R2C", r->id);
-    rc = do_whiten(s->wctx, r->d_spec, (unsigned)r->numbins);
-    if (!rc && (cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming) != cudaSuccess ||
-                cudaEventRecord(r->ready, s->astream) != cudaSuccess))
+    // the same transform as the context path (so a request's result equals
+    // accel_search's), on the admission stream
+    if (cudaEventCreate(&r->ev_prep) != cudaSuccess || cudaEventCreate(&r->ready) != cudaSuccess ||
+        cudaEventRecord(r->ev_prep, s->astream) != cudaSuccess)
+        return set_error(ACCEL_ERR_CUDA, "request %lld: event", r->id);
+    rc = do_rfft(s->wctx, r->d_series, r->n, r->d_spec);
+    if (!rc) rc = do_whiten(s->wctx, r->d_spec, (unsigned)r->numbins);
+    if (!rc && cudaEventRecord(r->ready, s->astream) != cudaSuccess)
         rc = set_error(ACCEL_ERR_CUDA, "request %lld: event", r->id);
     return rc;
 }
@@ -317,7 +325,12 @@ Flight launch_group(accel_server* s, int zmax, bool late_first) {
         return prio(s, a, c, now, late_first) < prio(s, b, c, now, late_first);
     });
     for (Request* r : order) {
+        if (r->next_step >= r->nsteps || !is_prepared(s, r)) continue;
+        // (its event has completed: this orders the group after it at no cost)
+        if (r->next_step == 0 && cudaStreamWaitEvent(s->stream, r->ready, 0) != cudaSuccess)
+            f.rc = set_error(ACCEL_ERR_CUDA, "request %lld: stream wait", r->id);
         while ((int)f.owner.size() < cap && r->next_step < r->nsteps) {
+            if (r->next_step == 0) r->t_first = now;
             SegDesc& d = B.h_segs[f.owner.size()];
             d.spec = r->d_spec;
             d.numbins = r->numbins;
@@ -346,8 +359,10 @@ Flight launch_group(accel_server* s, int zmax, bool late_first) {
         c->d_ncand = own_n;
     }
     cudaEventRecord(B.ev1, s->stream);
-    if (!f.rc && cudaMemcpyAsync(B.h_ncand, B.d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 s->stream) != cudaSuccess)
+    if (!f.rc && (cudaMemcpyAsync(B.h_ncand, B.d_ncand, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  s->stream) != cudaSuccess ||
+                  cudaMemcpyAsync(B.h_cands, B.d_cands, sizeof(RawCand) * std::min<long long>(kCandStage, c->cand_cap),
+                                  cudaMemcpyDeviceToHost, s->stream) != cudaSuccess))
         f.rc = set_error(ACCEL_ERR_CUDA, "server: group count");
     cudaEventRecord(B.done, s->stream);
     return f;
@@ -362,12 +377,38 @@ void complete_group(accel_server* s, Flight& f) {
     const long long half = (unsigned short)(c->uselen / 2);
     int rc = f.rc;
     std::vector<RawCand> raw;
+    const auto tw = Clock::now();
     if (!rc && cudaEventSynchronize(B.done) != cudaSuccess) rc = set_error(ACCEL_ERR_CUDA, "server: group");
+    {
+        const double ms = std::chrono::duration<double, std::milli>(Clock::now() - tw).count();
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->st.wait_ms += ms;
+        s->st.groups++;
+        s->st.group_segments += f.n;
+    }
+    if (!rc) {
+        // the group stream between the previous group's kernels and this
+        // one's: the GPU waiting on the host (or, after the queue had
+        // drained, on arrivals)
+        float gap = 0.f;
+        if (s->last_ev1 && cudaEventElapsedTime(&gap, s->last_ev1, B.ev0) == cudaSuccess && gap > 0.f) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            (f.after_idle ? s->st.idle_ms : s->st.gap_ms) += gap;
+        }
+        s->last_ev1 = B.ev1;
+    } else {
+        s->last_ev1 = nullptr;
+    }
     if (!rc && B.h_ncand[1]) rc = set_error(ACCEL_ERR_CUDA, "server: a harmonic-sum tile's copy wait timed out");
     if (!rc) {
         const long long nr = (long long)std::min<unsigned long long>(B.h_ncand[0], (unsigned long long)c->cand_cap);
         raw.resize(nr);
-        if (nr > 0 && cudaMemcpy(raw.data(), B.d_cands, sizeof(RawCand) * nr, cudaMemcpyDeviceToHost) != cudaSuccess)
+        const long long ns = std::min<long long>(nr, kCandStage);
+        if (ns > 0) std::memcpy(raw.data(), B.h_cands, sizeof(RawCand) * ns);
+        // (the group's kernels are done; a copy on the group stream would wait
+        // for the groups queued behind it)
+        if (nr > ns && cudaMemcpy(raw.data() + ns, B.d_cands + ns, sizeof(RawCand) * (nr - ns),
+                                  cudaMemcpyDeviceToHost) != cudaSuccess)
             rc = set_error(ACCEL_ERR_CUDA, "server: candidates");
         if (B.h_ncand[0] > (unsigned long long)c->cand_cap) rc = set_error(ACCEL_ERR_CAPACITY, "server: candidates");
         float ms = 0.f;
@@ -412,77 +453,20 @@ void complete_group(accel_server* s, Flight& f) {
     g.active.swap(keep);
 }
 
-// Makes the R2C plans of submitted lengths; destroys plans no request
-// needs while more than kPlanCache exist.
-void planner_loop(accel_server* s) {
-    cudaSetDevice(s->cfg.device);
-    for (;;) {
-        long long n = -1;
-        std::vector<cufftHandle> drop;
-        {
-            std::unique_lock<std::mutex> lk(s->plan_mu);
-            s->plan_cv.wait(lk, [&] { return s->plan_stop || !s->plan_queue.empty() || s->plan_evict; });
-            s->plan_evict = false;
-            if (!s->plan_queue.empty()) {
-                n = s->plan_queue.front();
-                s->plan_queue.pop_front();
-            } else if (s->plan_stop) {
-                return;
-            }
-            for (auto it = s->plans.begin(); it != s->plans.end() && s->plans.size() > kPlanCache;) {
-                if (s->plan_users.count(it->first) == 0) {
-                    if (it->second.ok) drop.push_back(it->second.plan);
-                    it = s->plans.erase(it);
-                } else {
-                    ++it;
-                }
-            }
-        }
-        for (cufftHandle h : drop) cufftDestroy(h);
-        if (n < 0) continue;
-        R2CPlan pl;
-        cufftResult e = cufftCreate(&pl.plan);
-        if (e == CUFFT_SUCCESS) e = cufftSetAutoAllocation(pl.plan, 0);
-        if (e == CUFFT_SUCCESS) e = cufftMakePlan1d(pl.plan, (int)n, CUFFT_R2C, 1, &pl.work);
-        pl.ok = e == CUFFT_SUCCESS;
-        if (!pl.ok && pl.plan) {
-            cufftDestroy(pl.plan);
-            pl.plan = 0;
-        }
-        {
-            std::lock_guard<std::mutex> lk(s->plan_mu);
-            s->plans[n] = pl;
-            s->planning.erase(n);
-        }
-        s->plan_cv.notify_all();
-        { std::lock_guard<std::mutex> lk(s->mu); }  // the worker waits on cv_work under mu
-        s->cv_work.notify_all();
-    }
-}
-
-// Admission thread: admits queued requests in arrival order as their R2C
-// plans become ready (a request whose plan is still being made does not
-// hold back the ones behind it) while the HBM budget and the active limit
-// allow, stopping at the first request they cannot take; prepares each
-// on the admission stream and hands it to the scheduler.
+// Admission thread: admits queued requests in arrival order while the HBM
+// budget and the active limit allow, stopping at the first request they
+// cannot take; prepares each on the admission stream and hands it to the
+// scheduler.
 void admitter_loop(accel_server* s) {
     cudaSetDevice(s->cfg.device);
     for (;;) {
         std::vector<Request*> admitted;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            // lock order: mu, then plan_mu
-            auto plan_ready = [&](const Request* r) {
-                std::lock_guard<std::mutex> pk(s->plan_mu);
-                return s->plans.count(r->n) != 0;
-            };
             auto can_admit = [&] {
-                for (const Request* r : s->pending) {
-                    if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) return false;
-                    if (s->bytes_in_use + r->bytes > s->cfg.hbm_budget_bytes) return false;
-                    if (plan_ready(r)) return true;
-                }
-                return false;
+                if (s->pending.empty()) return false;
+                if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) return false;
+                return s->bytes_in_use + s->pending.front()->bytes <= s->cfg.hbm_budget_bytes;
             };
             s->cv_work.wait(lk, [&] { return (s->stop && s->pending.empty()) || can_admit(); });
             if (s->stop && s->pending.empty()) {
@@ -490,15 +474,11 @@ void admitter_loop(accel_server* s) {
                 s->cv_work.notify_all();
                 return;
             }
-            for (auto it = s->pending.begin(); it != s->pending.end();) {
-                Request* r = *it;
+            while (!s->pending.empty()) {
+                Request* r = s->pending.front();
                 if (s->cfg.max_active > 0 && s->st.active >= s->cfg.max_active) break;
                 if (s->bytes_in_use + r->bytes > s->cfg.hbm_budget_bytes) break;
-                if (!plan_ready(r)) {
-                    ++it;
-                    continue;
-                }
-                it = s->pending.erase(it);
+                s->pending.pop_front();
                 s->bytes_in_use += r->bytes;
                 s->st.admitted++;
                 s->st.active++;
@@ -509,9 +489,11 @@ void admitter_loop(accel_server* s) {
         }
         for (Request* r : admitted) {
             const auto ta = Clock::now();
+            r->t_admit = ta;
             const int rc = admit(s, r);
             {
-                const double ms = std::chrono::duration<double, std::milli>(Clock::now() - ta).count();
+                r->t_prepared = Clock::now();
+                const double ms = std::chrono::duration<double, std::milli>(r->t_prepared - ta).count();
                 std::lock_guard<std::mutex> lk(s->mu);
                 s->st.admit_ms += ms;
             }
@@ -550,9 +532,6 @@ void worker_loop(accel_server* s) {
         for (Request* r : incoming) {
             int rc = ACCEL_OK;
             accel_ctx* c = group_ctx(s, r->zmax, &rc);
-            // the group stream waits for the request's copy, R2C and whitening
-            if (c && cudaStreamWaitEvent(s->stream, r->ready, 0) != cudaSuccess)
-                rc = set_error(ACCEL_ERR_CUDA, "request %lld: stream wait", r->id);
             if (!c || rc) {
                 finish(s, r, rc ? rc : ACCEL_ERR_CUDA, s->stream);
                 continue;
@@ -576,13 +555,13 @@ void worker_loop(accel_server* s) {
         bool any_late = false;
         for (auto& kv : s->groups)
             for (Request* r : kv.second.active)
-                any_late |= r->next_step < r->nsteps && is_late(s, r, now);
+                any_late |= r->next_step < r->nsteps && is_late(s, r, now) && is_prepared(s, r);
         const bool late_first = any_late && s->late_turn;
         if (any_late) s->late_turn = !s->late_turn;
         for (auto& kv : s->groups) {
             accel_ctx* c = kv.second.ctx;
             for (Request* r : kv.second.active) {
-                if (r->next_step >= r->nsteps) continue;
+                if (r->next_step >= r->nsteps || !is_prepared(s, r)) continue;
                 const Prio p = prio(s, r, c, now, late_first);
                 if (zmax < 0 || p < best) {
                     zmax = kv.first;
@@ -597,16 +576,24 @@ void worker_loop(accel_server* s) {
         const auto tg = Clock::now();
         Flight next;
         if (zmax >= 0) next = launch_group(s, zmax, late_first);
+        const double launch_ms = std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
         const bool launched = next.n > 0;
-        if (launched) s->flights.push_back(std::move(next));
+        if (launched) {
+            next.after_idle = s->flights.empty();
+            s->flights.push_back(std::move(next));
+        }
         if (!s->flights.empty() && ((int)s->flights.size() >= kFlightDepth || !launched)) {
             complete_group(s, s->flights.front());
             s->flights.pop_front();
+        } else if (!launched && s->flights.empty()) {
+            // nothing to launch or read: wait for a request still being prepared
+            if (Request* r = first_unprepared(s)) cudaEventSynchronize(r->ready);
         }
         {
             const double ms = std::chrono::duration<double, std::milli>(Clock::now() - tg).count();
             std::lock_guard<std::mutex> lk(s->mu);
             s->st.group_ms += ms;
+            s->st.launch_ms += launch_ms;
         }
     }
 }
@@ -644,8 +631,9 @@ int accel_server_create(const accel_server_config* cfg, accel_server** out) {
         delete s;
         return set_error(ACCEL_ERR_CUDA, "accel_server_create: %s", cudaGetErrorString(e));
     }
-    // whitening for the admission thread: a context of its own (its plans
-    // cache is not shared with the scheduler's contexts), on its stream
+    // R2C and whitening for the admission thread: a context of its own (its
+    // transform plans and whitening plans are not shared with the
+    // scheduler's contexts), on its stream
     accel_config wc;
     accel_config_init(&wc);
     wc.zmax = 0;
@@ -662,7 +650,15 @@ int accel_server_create(const accel_server_config* cfg, accel_server** out) {
         delete s;
         return rc;
     }
-    for (int i = 0; i < kPlanners; i++) s->planners.emplace_back(planner_loop, s);
+    // pinned staging for the series copies (without it: copies from pageable memory)
+    for (int k = 0; k < 2; k++) {
+        if (cudaMallocHost(&s->stage[k], sizeof(float) * kStageFloats) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->stage_ev[k], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            if (s->stage[k]) cudaFreeHost(s->stage[k]);
+            s->stage[k] = nullptr;
+        }
+    }
     s->admitter = std::thread(admitter_loop, s);
     s->worker = std::thread(worker_loop, s);
     *out = s;
@@ -678,19 +674,8 @@ int accel_server_destroy(accel_server* s) {
     s->cv_work.notify_all();
     if (s->admitter.joinable()) s->admitter.join();
     if (s->worker.joinable()) s->worker.join();
-    {
-        std::lock_guard<std::mutex> lk(s->plan_mu);
-        s->plan_stop = true;
-        s->plan_queue.clear();
-    }
-    s->plan_cv.notify_all();
-    for (std::thread& t : s->planners)
-        if (t.joinable()) t.join();
     cudaStreamSynchronize(s->stream);
     cudaStreamSynchronize(s->astream);
-    for (auto& kv : s->plans)
-        if (kv.second.ok) cufftDestroy(kv.second.plan);
-    cudaFree(s->work);
     for (auto& kv : s->groups) free_group(kv.second);
     for (auto& kv : s->reqs) {
         if (kv.second->d_series) cudaFree(kv.second->d_series);
@@ -698,6 +683,10 @@ int accel_server_destroy(accel_server* s) {
         if (kv.second->ready) cudaEventDestroy(kv.second->ready);
     }
     accel_destroy(s->wctx);
+    for (int k = 0; k < 2; k++) {
+        if (s->stage[k]) cudaFreeHost(s->stage[k]);
+        if (s->stage_ev[k]) cudaEventDestroy(s->stage_ev[k]);
+    }
     cudaStreamDestroy(s->astream);
     cudaStreamDestroy(s->stream);
     delete s;
@@ -719,13 +708,6 @@ int accel_server_submit(accel_server* s, const float* series, long long n, doubl
     if (r->bytes > s->cfg.hbm_budget_bytes)
         return set_error(ACCEL_ERR_BUDGET, "request of %.3g bytes exceeds the HBM budget of %.3g", r->bytes,
                          s->cfg.hbm_budget_bytes);
-    {
-        // the planner makes this length's R2C plan while the request waits
-        std::lock_guard<std::mutex> lk(s->plan_mu);
-        s->plan_users[n]++;
-        if (s->plans.count(n) == 0 && s->planning.insert(n).second) s->plan_queue.push_back(n);
-    }
-    s->plan_cv.notify_all();
     {
         std::lock_guard<std::mutex> lk(s->mu);
         r->id = s->next_id++;
@@ -766,6 +748,23 @@ int accel_server_result(accel_server* s, long long id, accel_candidate* out, lon
     const long long m = std::min<long long>(cap, (long long)r->cands.size());
     if (out && m > 0) std::memcpy(out, r->cands.data(), sizeof(accel_candidate) * m);
     return r->state == 3 ? r->rc : ACCEL_OK;
+}
+
+int accel_server_timing(accel_server* s, long long id, double* out_ms) {
+    if (!s || !out_ms) return set_error(ACCEL_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return set_error(ACCEL_ERR_INVALID, "unknown request %lld", id);
+    const Request* r = it->second.get();
+    if (r->state != 2) return set_error(ACCEL_ERR_INVALID, "request %lld has not completed", id);
+    auto ms = [](Clock::time_point a, Clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    out_ms[0] = ms(r->t_submit, r->t_admit);
+    out_ms[1] = ms(r->t_admit, r->t_prepared);
+    out_ms[2] = r->nsteps ? ms(r->t_prepared, r->t_first) : 0.0;
+    out_ms[3] = r->nsteps ? ms(r->t_first, r->t_done) : ms(r->t_prepared, r->t_done);
+    return ACCEL_OK;
 }
 
 int accel_server_release(accel_server* s, long long id) {

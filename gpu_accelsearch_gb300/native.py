@@ -52,7 +52,11 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
                 ("completed", C.c_longlong), ("queued", C.c_longlong), ("active", C.c_longlong),
                 ("bytes_in_use", C.c_double), ("cells", C.c_longlong), ("gpu_ms", C.c_double),
-                ("admit_ms", C.c_double), ("group_ms", C.c_double)]
+                ("admit_ms", C.c_double), ("group_ms", C.c_double), ("gap_ms", C.c_double),
+                ("idle_ms", C.c_double), ("wait_ms", C.c_double), ("launch_ms", C.c_double),
+                ("prep_gpu_ms", C.c_double),
+                ("groups", C.c_longlong),
+                ("group_segments", C.c_longlong)]
 
 
 class Tuning(C.Structure):
@@ -145,6 +149,7 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)]),
     "accel_server_release": (C.c_int, [_vp, _ll]),
     "accel_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+    "accel_server_timing": (C.c_int, [_vp, _ll, C.POINTER(C.c_double)]),
     "accel_dedisperse_delays": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double,
                                           C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int)]),

@@ -67,6 +67,15 @@ class Server:
             out[i] = (c.trial, c.step, c.r, c.z, c.numharm, c.power, c.sigma)
         return out, lat.value
 
+    def timing(self, rid: int) -> dict:
+        """Latency breakdown (ms) of a completed request: queue (submission to
+        admission), prepare (admission's copy, transform and whitening
+        launches), wait (prepared to its first launch group), search (first
+        launch group to completion)."""
+        out = (C.c_double * 4)()
+        N.check(N.lib().accel_server_timing(self._h, rid, out))
+        return dict(zip(("queue_ms", "prepare_ms", "wait_ms", "search_ms"), list(out)))
+
     def release(self, rid: int):
         N.check(N.lib().accel_server_release(self._h, rid))
         self._keep.pop(rid, None)

@@ -278,7 +278,10 @@ int  accel_whiten_blocks(long long numbins, int initbuf, int maxbuf, int *start,
  * cuda_stream may be NULL (the legacy default stream). */
 int  accel_whiten_noalloc(accel_complex *spec_dev, long long numbins, int initbuf, int maxbuf,
                           void *cuda_stream);
-/* Real-to-complex FFT of a device series into spec_dev (n/2+1 bins). */
+/* Real-to-complex FFT of a device series into spec_dev (n/2+1 bins), n
+ * even.  Computed from power-of-two cuFFT plans only (the n/2 complex pairs
+ * by one C2C transform when n/2 is a power of two, else by Bluestein's
+ * chirp-z form), so that trials of many lengths make no plan per length. */
 int  accel_rfft(accel_ctx *ctx, const float *series_dev, long long n, accel_complex *spec_dev);
 /* Segment spectra of nseg steps (first bins startr[]): per step and
  * harmonic the M_h = L_h/2 point spectrum of the normalised segment, packed
@@ -302,10 +305,9 @@ int  accel_bank_spectra(const accel_ctx *ctx, int h, accel_complex *kstd, accel_
 
 /* ------------------------------------------------------------------ serving */
 /* A request server with continuous batching (no counterpart in the
- * reference, whose driver searches one trial per process run).  Planner
- * threads make each request's R2C plan when it is submitted; an admission
- * thread admits requests in arrival order, as their plans are ready, while
- * their device memory (series and spectrum, 12 bytes per sample) fits
+ * reference, whose driver searches one trial per process run).  An
+ * admission thread admits requests in arrival order while their device
+ * memory (series and spectrum, 12 bytes per sample) fits
  * hbm_budget_bytes, and copies, transforms and whitens them on its own
  * stream; a scheduler thread fills each launch group from one template
  * bank (one bank per zmax, built on first use), shortest remaining work
@@ -340,6 +342,18 @@ typedef struct accel_server_stats {
     double admit_ms;          /* admission-thread time (copy, R2C, whitening)  */
     double group_ms;          /* scheduler time launching and completing groups */
                               /* (includes waiting for the GPU)               */
+    double gap_ms;            /* GPU time between consecutive launch groups    */
+                              /* while later groups were already queued: the  */
+                              /* group stream waiting on the host (or on a    */
+                              /* new request's transform and whitening)       */
+    double idle_ms;           /* the same after the queue had drained: no step */
+                              /* was left to launch (waiting for arrivals)    */
+    double wait_ms;           /* part of group_ms blocked on groups' completion */
+    double launch_ms;         /* part of group_ms building and launching groups */
+    double prep_gpu_ms;       /* CUDA-event time of the requests' transforms and */
+                              /* whitening (admission stream)                */
+    long long groups;         /* launch groups read back                       */
+    long long group_segments; /* their overlap-save segments                   */
 } accel_server_stats;
 
 void accel_server_config_init(accel_server_config *cfg);
@@ -358,6 +372,12 @@ int  accel_server_wait(accel_server *srv, long long id, double timeout_s, int *d
 int  accel_server_result(accel_server *srv, long long id, accel_candidate *out, long long cap,
                          long long *n, double *latency_ms);
 int  accel_server_release(accel_server *srv, long long id);
+/* Latency breakdown of a completed request, milliseconds: [0] submission to
+ * admission (HBM budget, admission queue), [1] admission's host
+ * work (copy from the caller's memory, transform and whitening launches),
+ * [2] prepared to its first launch group, [3] first launch group to
+ * completion.  The four add up to the latency accel_server_result reports. */
+int  accel_server_timing(accel_server *srv, long long id, double out_ms[4]);
 int  accel_server_get_stats(accel_server *srv, accel_server_stats *out);
 
 /* ------------------------------------------------------- dedispersion */

@@ -75,8 +75,15 @@ def test_continuous_batching_short_request_overtakes():
         assert srv.wait(lid, 300)
         _, lat_long = srv.result(lid)
         _, lat_short = srv.result(sid)
+        parts = [srv.timing(lid), srv.timing(sid)]
+        st = srv.stats()
     assert long_running and short_done_first
     assert lat_short < lat_long
+    # the latency breakdown adds up to the latency, every part non-negative
+    for lat, p in zip((lat_long, lat_short), parts):
+        assert all(v >= 0 for v in p.values()), p
+        assert abs(sum(p.values()) - lat) < 1e-6 * lat + 1e-3, (p, lat)
+    assert st["gap_ms"] >= 0 and st["idle_ms"] >= 0
 
 
 def test_many_lengths_and_banks_equal_context_path():
