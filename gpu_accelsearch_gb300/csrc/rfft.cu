@@ -4,7 +4,11 @@
 //
 // The N real samples are read as K = N/2 complex values z[n] = x[2n] +
 // i x[2n+1].  Z = DFT_K(z) is one power-of-two C2C transform when K is a
-// power of two, else Bluestein's chirp-z form: with w[m] = exp(i pi m^2/K),
+// power of two; when K = m L with L a power of two and an odd m <= 15, m
+// transforms of L points (the samples j, j + m, j + 2m, ...) combined by
+//     Z[k] = sum_j exp(-2 pi i j k / K) Y_j[k mod L]
+// (one Cooley-Tukey step); else Bluestein's chirp-z form: with
+// w[m] = exp(i pi m^2/K),
 //     Z[k] = conj(w[k]) sum_n (z[n] conj(w[n])) w[k - n],
 // a linear convolution done by power-of-two transforms of P >= 2K - 1
 // points.  Every phase is a multiple of pi/K reduced exactly to r in
@@ -33,29 +37,70 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
 }
 
 // Phase tables of exp(i pi r / K): lo[t] for t < S, hi[q] = exp(i pi q S/K)
-// for q < ceil(2K/S), in double precision.
-__global__ void k_phase_tables(double2* __restrict__ lo, double2* __restrict__ hi, long long K, int S, int nq) {
+// for q < ceil(2K/S), in double precision and rounded to float.
+__global__ void k_phase_tables(double2* __restrict__ lo, double2* __restrict__ hi, float2* __restrict__ flo,
+                               float2* __restrict__ fhi, long long K, int S, int nq) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double s, c;
     if (i < S) {
         sincospi((double)i / (double)K, &s, &c);
         lo[i] = make_double2(c, s);
+        flo[i] = make_float2((float)c, (float)s);
     } else if (i < S + nq) {
         sincospi((double)(i - S) * (double)S / (double)K, &s, &c);
         hi[i - S] = make_double2(c, s);
+        fhi[i - S] = make_float2((float)c, (float)s);
     }
 }
 
 struct Phase {
     const double2* lo;
     const double2* hi;
+    const float2* flo;
+    const float2* fhi;
     unsigned S;
-    // exp(i pi r / K) for 0 <= r < 2K
+    // exp(i pi r / K) for 0 <= r < 2K: in double, and (f) in float
     __device__ __forceinline__ double2 operator()(unsigned r) const {
         const double2 a = hi[r / S], b = lo[r % S];
         return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
     }
+    __device__ __forceinline__ float2 f(unsigned r) const {
+        const float2 a = __ldg(fhi + r / S), b = __ldg(flo + r % S);
+        return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+    }
 };
+
+// T[j L + l] = z[j + m l]: the m subsequences of stride m, each contiguous
+__global__ void k_ct_split(const float2* __restrict__ z, float2* __restrict__ T, int m, long long L) {
+    const long long K = (long long)m * L;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < K;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long j = i / L, l = i - j * L;
+        T[i] = z[j + (long long)m * l];
+    }
+}
+
+// Z[k] = sum_j exp(-2 pi i j k / K) Y_j[k mod L], Y_j = T[j L .. j L + L)
+__global__ void k_ct_combine(const float2* __restrict__ T, float2* __restrict__ Z, int m, long long L,
+                             Phase ph) {
+    const long long K = (long long)m * L;
+    const unsigned long long K2 = 2ull * (unsigned long long)K;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long l = k & (L - 1);
+        float2 acc = T[l];
+        unsigned long long r = 0;  // 2 j k mod 2K, a multiple of pi/K
+        for (int j = 1; j < m; j++) {
+            r += 2ull * (unsigned long long)k;
+            if (r >= K2) r -= K2;
+            const float2 w = ph.f((unsigned)r);  // exp(+i pi r/K); the transform uses its conjugate
+            const float2 y = T[(long long)j * L + l];
+            acc.x += y.x * w.x + y.y * w.y;
+            acc.y += y.y * w.x - y.x * w.y;
+        }
+        Z[k] = acc;
+    }
+}
 
 // The chirp w[m] = exp(i pi m^2 / K) for m in [0, K), wrapped into b (b[m]
 // and b[P - m], zero elsewhere), and a[n] = z[n] conj(w[n]) for n < K,
@@ -122,6 +167,10 @@ __global__ void k_r2c_unpack(float2* __restrict__ X, long long K, Phase ph) {
     }
 }
 
+// Largest odd factor taken by the Cooley-Tukey step (its combine reads m
+// values per output)
+constexpr long long kCtMaxOdd = 15;
+
 int grid_for(long long n) {
     long long g = (n + 255) / 256;
     return (int)(g < 152 * 16 ? (g < 1 ? 1 : g) : 152 * 16);
@@ -182,9 +231,10 @@ int r2c_aligned(R2CEngine& e, const float* x, long long n, float2* out, cudaStre
     while ((long long)S * S < 2 * K) S <<= 1;
     const int nq = (int)((2 * K + S - 1) / S);
     double2* tab = nullptr;
-    if (cudaMallocAsync(&tab, sizeof(double2) * (S + nq), st) != cudaSuccess) return -2;
-    k_phase_tables<<<(S + nq + 255) / 256, 256, 0, st>>>(tab, tab + S, K, S, nq);
-    const Phase ph{tab, tab + S, (unsigned)S};
+    if (cudaMallocAsync(&tab, (sizeof(double2) + sizeof(float2)) * (S + nq), st) != cudaSuccess) return -2;
+    float2* ftab = reinterpret_cast<float2*>(tab + S + nq);
+    k_phase_tables<<<(S + nq + 255) / 256, 256, 0, st>>>(tab, tab + S, ftab, ftab + S, K, S, nq);
+    const Phase ph{tab, tab + S, ftab, ftab + S, (unsigned)S};
     const int rc = cudaGetLastError() != cudaSuccess ? -1 : r2c_tables(e, z, K, out, ph, st);
     cudaFreeAsync(tab, st);
     return rc;
@@ -197,6 +247,26 @@ int r2c_tables(R2CEngine& e, const float2* z, long long K, float2* out, const Ph
             cufftExecC2C(h, reinterpret_cast<cufftComplex*>(const_cast<float2*>(z)),
                          reinterpret_cast<cufftComplex*>(out), CUFFT_FORWARD) != CUFFT_SUCCESS)
             return -1;
+    } else if ((K >> __builtin_ctzll(K)) <= kCtMaxOdd) {
+        const int m = (int)(K >> __builtin_ctzll(K));
+        const long long L = K / m;
+        cufftHandle h = 0;
+        if (L > 1 && (c2c_plan(e, L, &h) || cufftSetStream(h, st) != CUFFT_SUCCESS)) return -1;
+        float2* T = nullptr;
+        if (cudaMallocAsync(&T, sizeof(float2) * K, st) != cudaSuccess) return -2;
+        int rc = 0;
+        k_ct_split<<<grid_for(K), 256, 0, st>>>(z, T, m, L);
+        if (cudaGetLastError() != cudaSuccess) rc = -1;
+        for (int j = 0; j < m && !rc && L > 1; j++)
+            if (cufftExecC2C(h, reinterpret_cast<cufftComplex*>(T + (long long)j * L),
+                             reinterpret_cast<cufftComplex*>(T + (long long)j * L), CUFFT_FORWARD) != CUFFT_SUCCESS)
+                rc = -1;
+        if (!rc) {
+            k_ct_combine<<<grid_for(K), 256, 0, st>>>(T, out, m, L, ph);
+            if (cudaGetLastError() != cudaSuccess) rc = -1;
+        }
+        cudaFreeAsync(T, st);
+        if (rc) return rc;
     } else {
         long long P = 1;
         while (P < 2 * K - 1) P <<= 1;

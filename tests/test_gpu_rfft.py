@@ -1,7 +1,9 @@
 """The real-to-complex transform of any even length from power-of-two cuFFT
-plans (accel_rfft): against numpy's double-precision rfft, for lengths whose
-half is a power of two (one C2C transform), a multiple of 3 or 7, a prime or
-tiny (Bluestein), and for a device series at an odd float offset."""
+plans (accel_rfft): against numpy's double-precision rfft and cuFFT's own
+single-precision R2C, for lengths whose half is a power of two (one C2C
+transform), an odd factor up to 15 times a power of two (Cooley-Tukey
+step), or anything else -- 17 * 2^9, a prime, a product of many primes
+(Bluestein) -- and for a device series at an odd float offset."""
 import numpy as np
 import pytest
 
@@ -32,8 +34,8 @@ def transform(S, x, offset=0):
     return got
 
 
-@pytest.mark.parametrize("n", [2, 4, 6, 14, 1 << 10, 1 << 20, 3 << 19, 7 * 9 * 25 * 64, 2 * 1000003,
-                               2 * 3 * 5 * 7 * 11 * 13 * 17])
+@pytest.mark.parametrize("n", [2, 4, 6, 14, 30, 1 << 10, 1 << 20, 3 << 19, 5 << 17, 7 << 15, 9 << 12, 15 << 14,
+                               17 << 10, 7 * 9 * 25 * 64, 2 * 1000003, 2 * 3 * 5 * 7 * 11 * 13 * 17])
 def test_rfft_any_length(S, n):
     x = synth_series(n, seed=n % 1000 + 3, signals=[(0.05, n / 7.3, 0.0)]) if n >= 64 else \
         np.random.default_rng(n).standard_normal(n).astype(np.float32)
