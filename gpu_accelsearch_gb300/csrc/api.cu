@@ -17,6 +17,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/accelsearch.h"
@@ -803,10 +804,19 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
     unsigned long long nraw = *c->h_ncand;
     c->last_raw = nraw;
     long long keep = (long long)std::min<unsigned long long>(nraw, (unsigned long long)c->cand_cap);
-    std::vector<RawCand> raw(keep);
+    if (keep > c->h_raw_cap) {
+        // pinned, so that the read-back is one asynchronous DMA
+        const long long cap = std::max(keep, 2 * c->h_raw_cap);
+        CK(cudaStreamSynchronize(c->stream));
+        cudaFreeHost(c->h_raw);
+        c->h_raw = nullptr;
+        c->h_raw_cap = 0;
+        CK(cudaMallocHost(&c->h_raw, sizeof(RawCand) * cap));
+        c->h_raw_cap = cap;
+    }
+    const RawCand* raw = c->h_raw;
     if (keep > 0)
-        CK(cudaMemcpyAsync(raw.data(), c->d_cands, sizeof(RawCand) * keep, cudaMemcpyDeviceToHost,
-                           c->stream));
+        CK(cudaMemcpyAsync(c->h_raw, c->d_cands, sizeof(RawCand) * keep, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaEventRecord(c->ev_end, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     {
@@ -815,27 +825,59 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         c->stats.searches++;
     }
     prof_collect(c);
-    c->results.clear();
-    c->results.reserve(keep);
-    for (const RawCand& r : raw) {
-        const SegDesc& d = c->h_segs[r.seg];
-        accel_candidate o;
-        o.trial = d.trial;
-        o.step = d.step;
-        o.r = (double)d.startr + 0.5 * r.ridx;
-        o.z = (double)(c->zlo0 + kDz * r.zidx);
-        o.numharm = r.numharm;
-        o.power = r.power;
-        o.sigma = (float)sigma_of_power(r.power, r.numharm, c->cfg.numindep);
-        c->results.push_back(o);
+    // Candidates in (trial, step, numharm, z, r) order.  Segment k holds
+    // (trial, step) in increasing order, so a counting sort by segment and
+    // a sort of each segment's few candidates by (numharm, z, r) give that
+    // order (no two candidates share all five keys); the conversion (sigma
+    // by Newton steps) and the per-segment sorts run on host threads.
+    std::vector<long long> off(total + 1, 0);
+    for (long long j = 0; j < keep; j++) off[raw[j].seg + 1]++;
+    for (long long s = 0; s < total; s++) off[s + 1] += off[s];
+    std::vector<long long> at(off.begin(), off.end() - 1);
+    std::vector<int> order(keep);
+    for (long long j = 0; j < keep; j++) order[at[raw[j].seg]++] = (int)j;
+    c->results.resize(keep);
+    accel_candidate* out = c->results.data();
+    const double numindep = c->cfg.numindep;
+    auto convert = [&](long long s0, long long s1) {
+        for (long long s = s0; s < s1; s++) {
+            const SegDesc& d = c->h_segs[s];
+            for (long long q = off[s]; q < off[s + 1]; q++) {
+                const RawCand& r = raw[order[q]];
+                accel_candidate& o = out[q];
+                o.trial = d.trial;
+                o.step = d.step;
+                o.r = (double)d.startr + 0.5 * r.ridx;
+                o.z = (double)(c->zlo0 + kDz * r.zidx);
+                o.numharm = r.numharm;
+                o.power = r.power;
+                o.sigma = (float)sigma_of_power(r.power, r.numharm, numindep);
+            }
+            std::sort(out + off[s], out + off[s + 1], [](const accel_candidate& a, const accel_candidate& b) {
+                if (a.numharm != b.numharm) return a.numharm < b.numharm;
+                if (a.z != b.z) return a.z < b.z;
+                return a.r < b.r;
+            });
+        }
+    };
+    const int nthr = keep < 16384 ? 1 : (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (nthr == 1) {
+        convert(0, total);
+    } else {
+        // segment ranges holding about keep / nthr candidates each
+        std::vector<std::thread> pool;
+        long long s0 = 0;
+        for (int t = 0; t < nthr && s0 < total; t++) {
+            const long long goal = keep * (t + 1) / nthr;
+            long long s1 = t == nthr - 1 ? total
+                                         : (long long)(std::upper_bound(off.begin(), off.end(), goal) - off.begin()) - 1;
+            s1 = std::max(s1, s0 + 1);
+            s1 = std::min(s1, total);
+            pool.emplace_back(convert, s0, s1);
+            s0 = s1;
+        }
+        for (std::thread& th : pool) th.join();
     }
-    std::sort(c->results.begin(), c->results.end(), [](const accel_candidate& a, const accel_candidate& b) {
-        if (a.trial != b.trial) return a.trial < b.trial;
-        if (a.step != b.step) return a.step < b.step;
-        if (a.numharm != b.numharm) return a.numharm < b.numharm;
-        if (a.z != b.z) return a.z < b.z;
-        return a.r < b.r;
-    });
     if (nraw > (unsigned long long)c->cand_cap)
         return set_err(ACCEL_ERR_CAPACITY, "%llu candidates exceed the capacity of %lld", nraw,
                        c->cand_cap);
@@ -886,6 +928,7 @@ void free_ctx(accel_ctx* c) {
     cudaFree(c->d_cands);
     cudaFree(c->d_ncand);
     cudaFreeHost(c->h_ncand);
+    cudaFreeHost(c->h_raw);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

@@ -103,6 +103,8 @@ struct accel_ctx {
     RawCand* d_cands = nullptr;
     unsigned long long* d_ncand = nullptr;
     unsigned long long* h_ncand = nullptr;  // pinned
+    RawCand* h_raw = nullptr;               // pinned read-back of the raw candidates
+    long long h_raw_cap = 0;
     long long cand_cap = 0;
 
     std::map<unsigned, WhitenPlanDev> wplans;  // by spectrum length, at most kWhitenPlans
