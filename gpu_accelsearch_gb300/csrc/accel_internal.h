@@ -5,6 +5,7 @@
 
 #include <atomic>
 
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -108,6 +109,19 @@ struct HsumArgs {
     int tile_floats;          // largest shared-memory footprint of a tile (host-proven)
     unsigned test_extra_tx;   // 0, or (failure-detection test) bytes each tile expects
                               // beyond its copies, so that its bounded wait runs out
+    // tensor path of the tiled sum (use_tmap): each harmonic's rectangle as
+    // one box of box_h rows x 4 box_w4 columns at box_off floats (128-byte
+    // aligned) in shared memory, box_tx bytes per tile in all
+    int use_tmap;
+    int box_w4[kMaxHarm], box_h[kMaxHarm], box_off[kMaxHarm];
+    unsigned box_tx;
+};
+
+// Tensor maps of one plane buffer, harmonic by harmonic: 3-D (columns,
+// f-dot rows, segments) views of each harmonic's planes for the tiled sum's
+// box copies (kernel parameter space).
+struct alignas(64) HsumMaps {
+    CUtensorMap m[kMaxHarm];
 };
 
 // Fundamental plane fused with the harmonic sum (k_fund_sum).
@@ -175,7 +189,7 @@ int launch_bank_build(const BankHarmDev* hd_dev, const BankHarmDev* hd_host, int
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
 int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st);
-int launch_hsum_tile(const HsumArgs& a, int nseg, int tile_rows, cudaStream_t st);
+int launch_hsum_tile(const HsumArgs& a, int nseg, int tile_rows, const HsumMaps* maps, cudaStream_t st);
 int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st);
 // Tile geometry of launch_hsum_tile (the host proves the shared-memory bound).
 constexpr int kHsumTileZ = 16;

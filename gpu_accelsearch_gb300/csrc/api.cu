@@ -7,6 +7,7 @@
 // of trials, keeps their spectra on the device, and runs the steps of all
 // of them in launch groups of `chunk` segments: segment preparation, the
 // fused plane kernel and the harmonic sum, with no host round trip.
+#include <cudaTypedefs.h>
 #include <cufft.h>
 
 #include <algorithm>
@@ -297,6 +298,7 @@ int build_plan(accel_ctx* c) {
     for (int k = 0; k < 3; k++) {
         const int TZ = kHsumTileRows[k];
         int worst = 0;
+        int bw4[kMaxHarm] = {}, bh[kMaxHarm] = {};  // largest rectangle of each harmonic
         for (long long ph = 0; ph < 4LL * qmax && worst < (1 << 30); ph++) {
             const long long startr = 1000000 + ph;
             for (int z0 = 0; z0 < c->numzs0; z0 += TZ) {
@@ -321,6 +323,8 @@ int build_plan(accel_ctx* c) {
                             break;
                         }
                         off += 4 * (zl - zf + 1) * w4;
+                        bw4[h] = std::max(bw4[h], w4);
+                        bh[h] = std::max(bh[h], zl - zf + 1);
                     }
                     worst = std::max(worst, off);
                 }
@@ -328,10 +332,66 @@ int build_plan(accel_ctx* c) {
         }
         c->tile_floats_h[k] = worst;
         c->tile_ok_h[k] = worst <= hsum_tile_floats_max(TZ);
+        // boxes of the tensor path: every harmonic's largest rectangle, at
+        // 128-byte aligned offsets; a box dimension is at most 256 elements
+        int at = 0;
+        unsigned tx = 0;
+        bool fits = c->tile_ok_h[k];
+        for (int h = 0; h < c->nh; h++) {
+            c->tbox_w4[k][h] = bw4[h];
+            c->tbox_h[k][h] = bh[h];
+            c->tbox_off[k][h] = at;
+            at += (4 * bw4[h] * bh[h] + 31) & ~31;
+            tx += 16u * (unsigned)(bw4[h] * bh[h]);
+            fits = fits && bw4[h] >= 1 && 4 * bw4[h] <= 256 && bh[h] >= 1 && bh[h] <= 256;
+        }
+        c->tbox_floats[k] = at;
+        c->tbox_tx[k] = tx;
+        c->tbox_ok[k] = fits && at <= hsum_tile_floats_max(TZ);
     }
     c->tile_floats = c->tile_floats_h[1];  // 16 rows: the pipelined and persistent sums
     c->tile_ok = c->tile_ok_h[1];
     return ACCEL_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver (no link against libcuda), or null.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Tensor maps of the tiled sum's boxes for both plane buffers: harmonic h
+// as a 3-D tensor (prow_h columns, numzs_h rows, chunk segments; strides
+// prow_h and pstride floats) starting at its plane offset.  A plan, height
+// or buffer whose maps cannot be made takes the per-row bulk copies.
+void encode_hsum_maps(accel_ctx* c) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    float* bufs[2] = {c->planes, c->planes2};
+    for (int b = 0; b < 2; b++)
+        for (int k = 0; k < 3; k++) {
+            bool ok = enc && bufs[b] && c->tbox_ok[k];
+            for (int h = 0; h < c->nh && ok; h++) {
+                const HarmPlan& H = c->hp[h];
+                const cuuint64_t dim[3] = {(cuuint64_t)H.prow, (cuuint64_t)H.numzs, (cuuint64_t)c->chunk};
+                const cuuint64_t stride[2] = {(cuuint64_t)H.prow * 4, (cuuint64_t)c->pstride * 4};
+                const cuuint32_t box[3] = {(cuuint32_t)(4 * c->tbox_w4[k][h]), (cuuint32_t)c->tbox_h[k][h], 1};
+                const cuuint32_t estr[3] = {1, 1, 1};
+                ok = enc(&c->tmaps[b][k].m[h], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, bufs[b] + H.poff, dim, stride,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            }
+            c->tmaps_ok[b][k] = ok;
+        }
 }
 
 int alloc_work(accel_ctx* c) {
@@ -356,6 +416,7 @@ int alloc_work(accel_ctx* c) {
     // [0] candidate count, [1] kernel error bits
     CK(cudaMalloc(&c->d_ncand, 2 * sizeof(unsigned long long)));
     CK(cudaMallocHost(&c->h_ncand, 2 * sizeof(unsigned long long)));
+    encode_hsum_maps(c);
     return ACCEL_OK;
 }
 
@@ -548,7 +609,22 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
             int k = c->tile_rows == 8 ? 0 : c->tile_rows == 32 ? 2 : 1;
             if (!c->tile_ok_h[k]) k = 1;
             ha.tile_floats = c->tile_floats_h[k];
-            CKL(launch_hsum_tile(ha, nseg, kHsumTileRows[k], sum_stream), "harmonic sum (tiled)");
+            // one box copy per harmonic where the planes are one of the
+            // context's two buffers and their maps exist
+            const int b = planes == c->planes ? 0 : planes == c->planes2 ? 1 : -1;
+            const HsumMaps* maps = nullptr;
+            if (c->hsum_tensor && b >= 0 && c->tmaps_ok[b][k]) {
+                maps = &c->tmaps[b][k];
+                ha.use_tmap = 1;
+                for (int h = 0; h < c->nh; h++) {
+                    ha.box_w4[h] = c->tbox_w4[k][h];
+                    ha.box_h[h] = c->tbox_h[k][h];
+                    ha.box_off[h] = c->tbox_off[k][h];
+                }
+                ha.box_tx = c->tbox_tx[k];
+                ha.tile_floats = c->tbox_floats[k];
+            }
+            CKL(launch_hsum_tile(ha, nseg, kHsumTileRows[k], maps, sum_stream), "harmonic sum (tiled)");
         }
         else
             CKL(launch_hsum(ha, nseg, sum_stream), "harmonic sum");
@@ -1082,6 +1158,7 @@ int accel_get_tuning(const accel_ctx* c, accel_tuning* t) {
     t->persistent = c->persistent;
     t->hsum_tile_rows = c->tile_rows;
     t->wait_test = c->wait_test;
+    t->hsum_row_copies = !c->hsum_tensor;
     return ACCEL_OK;
 }
 
@@ -1102,6 +1179,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
     c->persistent = t->persistent != 0;
     c->tile_rows = t->hsum_tile_rows ? t->hsum_tile_rows : 16;
     c->wait_test = t->wait_test != 0;
+    c->hsum_tensor = t->hsum_row_copies == 0;
     if (t->chunk_segments != c->chunk) {
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaStreamSynchronize(c->stream2));
@@ -1118,6 +1196,7 @@ int accel_set_tuning(accel_ctx* c, const accel_tuning* t) {
         CK(cudaMalloc(&c->planes, sizeof(float) * c->pstride * c->chunk));
         CK(cudaMalloc(&c->planes2, sizeof(float) * c->pstride * c->chunk));
         CK(cudaMalloc(&c->d_step, sizeof(unsigned) * ((size_t)c->chunk + 1)));
+        encode_hsum_maps(c);
     }
     return ACCEL_OK;
 }

@@ -95,6 +95,16 @@ struct accel_ctx {
     int tile_floats_h[3] = {0, 0, 0};     // worst tile of 8, 16, 32 rows (floats)
     bool tile_ok_h[3] = {false, false, false};
     int tile_rows = 16;                   // height of the tiled sum's tiles
+    // tensor path of the tiled sum: per tile height, each harmonic's box
+    // (the largest rectangle of any tile), and the tensor maps of the two
+    // plane buffers
+    int hsum_tensor = 1;                  // box copies where the plan allows them
+    int tbox_w4[3][kMaxHarm]{}, tbox_h[3][kMaxHarm]{}, tbox_off[3][kMaxHarm]{};
+    int tbox_floats[3] = {0, 0, 0};
+    unsigned tbox_tx[3] = {0, 0, 0};
+    bool tbox_ok[3] = {false, false, false};
+    HsumMaps tmaps[2][3]{};               // [plane buffer][tile height]
+    bool tmaps_ok[2][3] = {};
     float2* dbuf = nullptr;
     float* planes = nullptr;
     SegDesc* d_segs = nullptr;

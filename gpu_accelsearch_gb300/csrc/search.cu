@@ -33,7 +33,7 @@ int launch_hsum(const HsumArgs& a, int nseg, cudaStream_t st) {
 }
 
 template <int NH, bool SO, int TZ>
-static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t st) {
+static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, const HsumMaps& maps, cudaStream_t st) {
     static std::atomic<unsigned long long> attr{0};
     int dev = 0;
     if (attr_pending(attr, &dev)) {
@@ -44,16 +44,16 @@ static int hsum_tile_nh(const HsumArgs& a, dim3 grid, size_t smem, cudaStream_t 
             return -1;
         attr_set(attr, dev);
     }
-    k_hsum_tile<NH, SO, TZ><<<grid, kTileI, smem, st>>>(a);
+    k_hsum_tile<NH, SO, TZ><<<grid, kTileI, smem, st>>>(a, maps);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <int NH, bool SO>
-static int hsum_tile_tz(const HsumArgs& a, int tz, dim3 grid, size_t smem, cudaStream_t st) {
+static int hsum_tile_tz(const HsumArgs& a, int tz, dim3 grid, size_t smem, const HsumMaps& maps, cudaStream_t st) {
     switch (tz) {
-        case 8: return hsum_tile_nh<NH, SO, 8>(a, grid, smem, st);
-        case 16: return hsum_tile_nh<NH, SO, 16>(a, grid, smem, st);
-        case 32: return hsum_tile_nh<NH, SO, 32>(a, grid, smem, st);
+        case 8: return hsum_tile_nh<NH, SO, 8>(a, grid, smem, maps, st);
+        case 16: return hsum_tile_nh<NH, SO, 16>(a, grid, smem, maps, st);
+        case 32: return hsum_tile_nh<NH, SO, 32>(a, grid, smem, maps, st);
     }
     return -1;
 }
@@ -99,7 +99,11 @@ int launch_hsum_pipe(const HsumArgs& a, int nseg, cudaStream_t st) {
     return -1;
 }
 
-int launch_hsum_tile(const HsumArgs& a, int nseg, int tz, cudaStream_t st) {
+int launch_hsum_tile(const HsumArgs& a0, int nseg, int tz, const HsumMaps* maps, cudaStream_t st) {
+    static const HsumMaps no_maps{};
+    HsumArgs a = a0;
+    if (!maps) a.use_tmap = 0;
+    const HsumMaps& m = maps ? *maps : no_maps;
     dim3 grid((a.uselen + kTileI - 1) / kTileI, (a.numzs0 + tz - 1) / tz, nseg);
     // the plan's own worst tile of this height (host-proven to fit): a
     // smaller footprint fits more CTAs per SM (4 instead of 3 at zmax 200,
@@ -109,11 +113,11 @@ int launch_hsum_tile(const HsumArgs& a, int nseg, int tz, cudaStream_t st) {
     const size_t smem = sizeof(float) * floats;
     const bool so = a.stage_out != nullptr;
     switch (a.nh) {
-        case 1: return so ? hsum_tile_tz<1, true>(a, tz, grid, smem, st) : hsum_tile_tz<1, false>(a, tz, grid, smem, st);
-        case 2: return so ? hsum_tile_tz<2, true>(a, tz, grid, smem, st) : hsum_tile_tz<2, false>(a, tz, grid, smem, st);
-        case 4: return so ? hsum_tile_tz<4, true>(a, tz, grid, smem, st) : hsum_tile_tz<4, false>(a, tz, grid, smem, st);
-        case 8: return so ? hsum_tile_tz<8, true>(a, tz, grid, smem, st) : hsum_tile_tz<8, false>(a, tz, grid, smem, st);
-        case 16: return so ? hsum_tile_tz<16, true>(a, tz, grid, smem, st) : hsum_tile_tz<16, false>(a, tz, grid, smem, st);
+        case 1: return so ? hsum_tile_tz<1, true>(a, tz, grid, smem, m, st) : hsum_tile_tz<1, false>(a, tz, grid, smem, m, st);
+        case 2: return so ? hsum_tile_tz<2, true>(a, tz, grid, smem, m, st) : hsum_tile_tz<2, false>(a, tz, grid, smem, m, st);
+        case 4: return so ? hsum_tile_tz<4, true>(a, tz, grid, smem, m, st) : hsum_tile_tz<4, false>(a, tz, grid, smem, m, st);
+        case 8: return so ? hsum_tile_tz<8, true>(a, tz, grid, smem, m, st) : hsum_tile_tz<8, false>(a, tz, grid, smem, m, st);
+        case 16: return so ? hsum_tile_tz<16, true>(a, tz, grid, smem, m, st) : hsum_tile_tz<16, false>(a, tz, grid, smem, m, st);
     }
     return -1;
 }

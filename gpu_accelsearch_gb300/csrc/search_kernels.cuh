@@ -337,6 +337,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// One box of a 3-D tensor map (coordinates x = column, y = row, z =
+// segment) into shared memory (128-byte aligned); elements past the
+// tensor's edges arrive as zeros and count toward the transaction bytes.
+__device__ __forceinline__ void tensor_copy_g2s(void* sdst, const CUtensorMap* map, int x, int y, int z,
+                                                unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_addr(sdst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // bytes (a multiple of 16) from global to shared, both 16-byte aligned
 __device__ __forceinline__ void bulk_copy_g2s(void* sdst, const void* gsrc, unsigned bytes,
                                               unsigned long long* bar) {
@@ -365,10 +377,12 @@ template <int NH, int TZ = kTileZ> struct TileShared {
 // caller passes the parity of this use.  Returns false -- with the error
 // word set -- when the copies did not land within the bounded wait; the
 // barrier's state is then unknown and the CTA must not use it again.
+// With tensor maps (maps != null, a.use_tmap): one box copy per harmonic
+// instead of one bulk copy per rectangle row.
 template <int NH, bool STAGE_OUT, int TZ = kTileZ>
 __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z0, int i0, float* tsm,
                                                TileShared<NH, TZ>& S, unsigned long long* bar, bool init,
-                                               unsigned parity) {
+                                               unsigned parity, const CUtensorMap* maps = nullptr) {
     static_assert(NH <= 32, "one lane per harmonic");
     static_assert(TZ % 4 == 0 && TZ <= kTileI, "rows in batches of four, one thread per row table entry");
     const int nz = min(TZ, a.numzs0 - z0);
@@ -397,7 +411,8 @@ __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z
                 zl = sub_row(a.zlo0 + kDz * (z0 + nz - 1), H);
             }
             const int c0 = rfirst & ~3;
-            const int w4 = ((rlast - c0) >> 2) + 1;
+            // rectangle row pitch: its own width, or the harmonic's box
+            const int w4 = maps ? a.box_w4[h] : ((rlast - c0) >> 2) + 1;
             nzr = zl - zf + 1;
             S.zf[h] = zf;
             S.nzr[h] = nzr;
@@ -423,16 +438,20 @@ __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z
             }
         }
         if (tid < NH) {
-            S.off[tid] = incl - size;
+            S.off[tid] = maps ? a.box_off[tid] : incl - size;
             S.r0[tid] = rincl - nzr;  // first copy index of harmonic tid
         }
         const int total_floats = __shfl_sync(0xffffffffu, incl, 31);
         const int total_rows = __shfl_sync(0xffffffffu, rincl, 31);
         if (tid == 0) {
             if (init) mbar_init(bar, 1);
-            mbar_arrive_expect_tx(bar, 4u * (unsigned)total_floats + a.test_extra_tx);
+            mbar_arrive_expect_tx(bar, (maps ? a.box_tx : 4u * (unsigned)total_floats) + a.test_extra_tx);
         }
         __syncwarp();
+        if (maps) {
+            // lane h: harmonic h's box from (c0, zf) of segment seg
+            if (tid < NH) tensor_copy_g2s(tsm + S.off[tid], maps + tid, S.c0[tid], S.zf[tid], seg, bar);
+        } else
         for (int j = tid; j < total_rows; j += 32) {
             int h = 0;
 #pragma unroll
@@ -537,12 +556,13 @@ __device__ __forceinline__ bool hsum_tile_body(const HsumArgs& a, int seg, int z
 }
 
 template <int NH, bool STAGE_OUT, int TZ = kTileZ>
-__global__ void __launch_bounds__(kTileI, TZ > 16 ? 2 : 4) k_hsum_tile(const HsumArgs a) {
+__global__ void __launch_bounds__(kTileI, TZ > 16 ? 2 : 4)
+    k_hsum_tile(const HsumArgs a, const __grid_constant__ HsumMaps maps) {
     extern __shared__ __align__(128) float tsm[];
     __shared__ __align__(16) TileShared<NH, TZ> S;
     __shared__ __align__(8) unsigned long long s_bar;
     hsum_tile_body<NH, STAGE_OUT, TZ>(a, blockIdx.z, blockIdx.y * TZ, blockIdx.x * kTileI, tsm, S, &s_bar, true,
-                                      0u);
+                                      0u, a.use_tmap ? maps.m : nullptr);
 }
 
 // ------------------------------------------------------- pipelined tiled hsum

@@ -63,7 +63,7 @@ class Tuning(C.Structure):
     _fields_ = [("chunk_segments", C.c_int), ("plane_split", C.c_int), ("fused_sum", C.c_int),
                 ("hsum_rowwise", C.c_int), ("serial_sum", C.c_int), ("hsum_pipelined", C.c_int),
                 ("graph", C.c_int), ("hsum_tile_rows", C.c_int), ("persistent", C.c_int),
-                ("wait_test", C.c_int)]
+                ("hsum_row_copies", C.c_int), ("wait_test", C.c_int)]
 
 
 class Optimized(C.Structure):

@@ -198,11 +198,12 @@ class AccelSearch:
                 "fused_sum": t.fused_sum,
                 "hsum_rowwise": t.hsum_rowwise, "serial_sum": t.serial_sum,
                 "hsum_pipelined": t.hsum_pipelined, "graph": t.graph, "wait_test": t.wait_test,
-                "persistent": t.persistent, "hsum_tile_rows": t.hsum_tile_rows}
+                "persistent": t.persistent, "hsum_tile_rows": t.hsum_tile_rows,
+                "hsum_row_copies": t.hsum_row_copies}
 
     def set_tuning(self, chunk_segments=None, plane_split=None, fused_sum=None,
                    hsum_rowwise=None, serial_sum=None, hsum_pipelined=None, graph=None,
-                   wait_test=None, persistent=None, hsum_tile_rows=None):
+                   wait_test=None, persistent=None, hsum_tile_rows=None, hsum_row_copies=None):
         cur = self.tuning()
         t = N.Tuning()
         t.chunk_segments = cur["chunk_segments"] if chunk_segments is None else chunk_segments
@@ -215,6 +216,7 @@ class AccelSearch:
         t.wait_test = cur["wait_test"] if wait_test is None else int(wait_test)
         t.persistent = cur["persistent"] if persistent is None else int(persistent)
         t.hsum_tile_rows = cur["hsum_tile_rows"] if hsum_tile_rows is None else int(hsum_tile_rows)
+        t.hsum_row_copies = cur["hsum_row_copies"] if hsum_row_copies is None else int(hsum_row_copies)
         N.check(N.lib().accel_set_tuning(self._h, C.byref(t)))
 
     def profile(self, enable: bool = True):

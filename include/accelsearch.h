@@ -125,6 +125,10 @@ typedef struct accel_tuning {
                             /* rows are written (still in L2); segment lengths*/
                             /* other than 8192 and plans it cannot take fall  */
                             /* back to the separate kernels                   */
+    int hsum_row_copies;    /* 1: the tiled sum brings each rectangle in by   */
+                            /* one bulk copy per row; 0 (default): one 3-D   */
+                            /* tensor-map copy (TMA box) per harmonic where  */
+                            /* the plan's boxes fit                           */
     int wait_test;          /* failure-detection test, 0 in normal use: each  */
                             /* tile of the tiled harmonic sum expects 16      */
                             /* bytes that never arrive, so its bounded copy   */

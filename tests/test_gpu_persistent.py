@@ -5,7 +5,8 @@ float operations in the same order, so the candidate sets must be
 bit-identical -- at ~3.5 sigma cuts (thousands of candidates), over launch
 groups of 1 to 64 segments, FP32 and FP16 templates, graph and direct
 launches, and a batch of uneven trials.  The separate tiled sum at tile
-heights of 8 and 32 rows gives the same candidates too.  Its bounded waits are tested
+heights of 8, 16 and 32 rows, with tensor-map box copies or per-row bulk
+copies, gives the same candidates too.  Its bounded waits are tested
 without a GPU fault: with tuning.wait_test every tile's copy wait runs out,
 the search fails with ACCEL_ERR_CUDA and the context recovers."""
 import numpy as np
@@ -48,11 +49,14 @@ def test_persistent_equals_separate_kernels(zmax, numharm):
                 continue
             assert nstep > 0, chunk
             assert np.array_equal(got, base), chunk
-        # and the separate tiled sum at its other tile heights
-        for rows in (8, 32):
-            got, _ = search(s, d, w.size, 16, chunk_segments=16, persistent=0, hsum_tile_rows=rows)
-            assert np.array_equal(got, base), rows
-        s.set_tuning(hsum_tile_rows=16)
+        # and the separate tiled sum at its other tile heights, with its
+        # rectangles brought in by tensor-map boxes (default) or row copies
+        for rows in (8, 16, 32):
+            for row_copies in (0, 1):
+                got, _ = search(s, d, w.size, 16, chunk_segments=16, persistent=0, hsum_tile_rows=rows,
+                                hsum_row_copies=row_copies)
+                assert np.array_equal(got, base), (rows, row_copies)
+        s.set_tuning(hsum_tile_rows=16, hsum_row_copies=0)
 
 
 def test_persistent_fp16_graph_direct_and_batches():
