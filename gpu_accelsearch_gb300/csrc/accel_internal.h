@@ -9,6 +9,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <utility>
@@ -155,6 +157,37 @@ inline bool attr_pending(const std::atomic<unsigned long long>& done, int* dev) 
 }
 inline void attr_set(std::atomic<unsigned long long>& done, int dev) {
     if (dev < 64) done.fetch_or(1ull << dev);
+}
+
+// The smallest shared-memory carveout (percent of the SM's shared memory)
+// that holds as many CTAs of `kernel` as its registers and threads allow:
+// the rest of the unified L1/shared array stays L1 for the kernel's global
+// loads (the plane kernel: 2 CTAs of 70 KB take the 164 KB configuration,
+// leaving 92 KB of L1 instead of 28 KB at the largest carveout).
+inline int carveout_for(const void* kernel, int threads, size_t dyn_smem) {
+    cudaFuncAttributes fa{};
+    int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess ||
+        smem_sm <= 0 || threads <= 0) {
+        cudaGetLastError();
+        return 100;
+    }
+    const int regs = ((fa.numRegs + 7) & ~7) * threads;  // per CTA, in units of 8 registers a thread
+    int ctas = std::min(thr_sm / threads, regs > 0 ? regs_sm / regs : 32);
+    ctas = std::max(1, std::min(ctas, 32));
+    const double need = (double)ctas * ((double)dyn_smem + fa.sharedSizeBytes + reserved);
+    // the shared-memory capacities an SM of this family can be configured to
+    // (KB); the percent just below the chosen one lands on it whether the
+    // hint is rounded up or to the nearest capacity
+    if (smem_sm != 228 * 1024) return 100;
+    const int caps[] = {0, 8, 16, 32, 64, 100, 132, 164, 196, 228};
+    for (int cap : caps)
+        if (cap * 1024.0 >= need) return cap == 228 ? 100 : std::max(1, (int)std::floor(100.0 * cap / 228.0));
+    return 100;
 }
 
 // Candidate refinement (k_optimize in bank.cu): one CTA per candidate.

@@ -853,7 +853,7 @@ template <int M> static int prep_m(const PrepArgs& a, int nseg, const float2* tw
         if (cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_prep<M>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+                                 carveout_for((const void*)k_prep<M>, M / 16, smem)) != cudaSuccess)
             return -1;
         attr_set(attr, dev);
     }
@@ -870,7 +870,8 @@ static int plane_m(const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t 
         if (cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess ||
             cudaFuncSetAttribute(k_plane<M, F16, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+                                 carveout_for((const void*)k_plane<M, F16, SPLIT>, PlaneShape<SPLIT, M>::THREADS,
+                                              smem)) != cudaSuccess)
             return -1;
         attr_set(attr, dev);
     }
@@ -894,7 +895,8 @@ static int fund_m(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st
         if (cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess ||
             cudaFuncSetAttribute(k_fund_sum<M, F16>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+                                 carveout_for((const void*)k_fund_sum<M, F16>, PlaneShape<false, M>::THREADS,
+                                              smem)) != cudaSuccess)
             return -1;
         attr_set(attr, dev);
     }
