@@ -481,12 +481,12 @@ def measure_fp32_peak(torch) -> float:
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def load_traffic(kernel: str):
-    """DRAM bytes per segment of a kernel from the committed ncu summary
-    (profiles/dram_traffic_per_segment.json), or None."""
+def load_traffic(kernel: str, fftlen: int):
+    """DRAM bytes per segment of a kernel at segment length fftlen from the
+    committed ncu summary (profiles/dram_traffic_per_segment.json), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic_per_segment.json")) as f:
-            return float(json.load(f)[kernel]["dram_bytes_per_segment"])
+            return float(json.load(f)["by_fftlen"][str(fftlen)][kernel]["dram_bytes_per_segment"])
     except Exception:
         return None
 
@@ -670,7 +670,7 @@ def run_ours(args):
     names = {"plane": "k_plane (correlate + inverse FFT + |X|^2 power planes)",
              "hsum": "k_hsum_tile (harmonic sum + threshold over shared-memory tiles)",
              "fund": "k_fund_sum (fundamental plane fused with harmonic sum + threshold)"}
-    tr = load_traffic(dom) if dom else None
+    tr = load_traffic(dom, fftlen) if dom else None
     roofline = None
     import math
     # algorithmic FP32 work of one segment's plane rows: two M-point inverse
