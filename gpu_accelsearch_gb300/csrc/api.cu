@@ -906,8 +906,13 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
     // a sort of each segment's few candidates by (numharm, z, r) give that
     // order (no two candidates share all five keys); the conversion (sigma
     // by Newton steps) and the per-segment sorts run on host threads.
+    c->results.clear();
     std::vector<long long> off(total + 1, 0);
-    for (long long j = 0; j < keep; j++) off[raw[j].seg + 1]++;
+    for (long long j = 0; j < keep; j++) {
+        if (raw[j].seg < 0 || raw[j].seg >= total)
+            return set_err(ACCEL_ERR_CUDA, "candidate %lld names segment %d of %lld", j, raw[j].seg, total);
+        off[raw[j].seg + 1]++;
+    }
     for (long long s = 0; s < total; s++) off[s + 1] += off[s];
     std::vector<long long> at(off.begin(), off.end() - 1);
     std::vector<int> order(keep);
@@ -937,23 +942,27 @@ int run_search(accel_ctx* c, int ntrials, float2* const* spec, const long long* 
         }
     };
     const int nthr = keep < 16384 ? 1 : (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
-    if (nthr == 1) {
-        convert(0, total);
-    } else {
-        // segment ranges holding about keep / nthr candidates each
-        std::vector<std::thread> pool;
-        long long s0 = 0;
-        for (int t = 0; t < nthr && s0 < total; t++) {
-            const long long goal = keep * (t + 1) / nthr;
-            long long s1 = t == nthr - 1 ? total
-                                         : (long long)(std::upper_bound(off.begin(), off.end(), goal) - off.begin()) - 1;
-            s1 = std::max(s1, s0 + 1);
-            s1 = std::min(s1, total);
-            pool.emplace_back(convert, s0, s1);
-            s0 = s1;
+    // segment ranges holding about keep / nthr candidates each; a range a
+    // thread could not be started for is converted here
+    std::vector<std::thread> pool;
+    long long s0 = 0;
+    for (int t = 0; t < nthr && s0 < total; t++) {
+        const long long goal = keep * (t + 1) / nthr;
+        long long s1 = t == nthr - 1 ? total
+                                     : (long long)(std::upper_bound(off.begin(), off.end(), goal) - off.begin()) - 1;
+        s1 = std::min(std::max(s1, s0 + 1), total);
+        bool started = false;
+        if (t + 1 < nthr) {
+            try {
+                pool.emplace_back(convert, s0, s1);
+                started = true;
+            } catch (...) {
+            }
         }
-        for (std::thread& th : pool) th.join();
+        if (!started) convert(s0, s1);
+        s0 = s1;
     }
+    for (std::thread& th : pool) th.join();
     if (nraw > (unsigned long long)c->cand_cap)
         return set_err(ACCEL_ERR_CAPACITY, "%llu candidates exceed the capacity of %lld", nraw,
                        c->cand_cap);
