@@ -84,6 +84,10 @@ def test_continuous_batching_short_request_overtakes():
         assert all(v >= 0 for v in p.values()), p
         assert abs(sum(p.values()) - lat) < 1e-6 * lat + 1e-3, (p, lat)
     assert st["gap_ms"] >= 0 and st["idle_ms"] >= 0
+    # the scheduler's launch and wait time are parts of its group time; every
+    # launch group read back is counted with its segments
+    assert 0 <= st["launch_ms"] <= st["group_ms"] and 0 <= st["wait_ms"] <= st["group_ms"]
+    assert st["groups"] > 0 and st["group_segments"] >= st["groups"] and st["prep_gpu_ms"] > 0
 
 
 def test_many_lengths_and_banks_equal_context_path():
