@@ -1,5 +1,5 @@
-"""FP32 CPU restatement of the reference search (TEST INFRASTRUCTURE and CPU
-BASELINE ONLY: bench.py's cpu_baseline leg and --impl reference time it,
+"""FP32 CPU restatement of the reference search (test infrastructure and the
+CPU baseline only: bench.py's cpu_baseline leg and --impl reference time it,
 tests check it; the product library never imports it).
 
 It follows the reference pipeline's arithmetic and layout step by step,
