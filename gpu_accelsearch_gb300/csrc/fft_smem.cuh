@@ -73,23 +73,26 @@ template <int DIR> __device__ __forceinline__ float2 w8_3(float2 a) {
                    : make_float2(s * (a.y - a.x), -s * (a.x + a.y));
 }
 
+__device__ __forceinline__ float2 cfma(float s, float2 a, float2 b) {  // s a + b
+    return make_float2(fmaf(s, a.x, b.x), fmaf(s, a.y, b.y));
+}
+
+
+// 8 points as 2 x 4; the twiddles W8^1 = s (1 + i'), W8^3 = s (-1 + i')
+// (i' = DIR i, s = 1/sqrt2) applied by the fused multiply-adds of the last
+// layer: 52 floating-point instructions instead of 56.
 template <int DIR> __device__ __forceinline__ void dft8(float2* v) {
+    const float S = 0.70710678118654752440f;
     float2 e[4] = {v[0], v[2], v[4], v[6]};
     float2 o[4] = {v[1], v[3], v[5], v[7]};
     dft4<DIR>(e);
     dft4<DIR>(o);
-    o[1] = w8_1<DIR>(o[1]);
-    o[2] = mul_i<DIR>(o[2]);
-    o[3] = w8_3<DIR>(o[3]);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        v[k] = cadd(e[k], o[k]);
-        v[k + 4] = csub(e[k], o[k]);
-    }
-}
-
-__device__ __forceinline__ float2 cfma(float s, float2 a, float2 b) {  // s a + b
-    return make_float2(fmaf(s, a.x, b.x), fmaf(s, a.y, b.y));
+    const float2 p1 = cadd(o[1], mul_i<DIR>(o[1])), p3 = csub(mul_i<DIR>(o[3]), o[3]);
+    const float2 o2 = mul_i<DIR>(o[2]);
+    v[0] = cadd(e[0], o[0]), v[4] = csub(e[0], o[0]);
+    v[1] = cfma(S, p1, e[1]), v[5] = cfma(-S, p1, e[1]);
+    v[2] = cadd(e[2], o2), v[6] = csub(e[2], o2);
+    v[3] = cfma(S, p3, e[3]), v[7] = cfma(-S, p3, e[3]);
 }
 
 // 16 points as 4 x 4: x[4 n1 + n2] -> X[k1 + 4 k2].  DFT4 over n1 for each
