@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--serving-seconds", type=float, default=5.0,
                     help="duration of the Poisson arrival process of the serving leg (0: skip)")
     ap.add_argument("--serving-chunk", type=int, default=128, help="segments per launch group of the server")
+    ap.add_argument("--serving-max-chunk", type=int, default=0,
+                    help="largest launch group of the server, sized by the backlog (0: fixed groups)")
     ap.add_argument("--serving-lengths", default="log-uniform", choices=["log-uniform", "octaves"],
                     help="request lengths: log-uniform 2^18..2^23 (every request a new length), or "
                          "rounded down to powers of two")
@@ -161,7 +163,8 @@ def smooth_length(n: int) -> int:
             return m
         m += 2
 
-def run_serving(seconds: float, device: int, rate: float = 200.0, chunk: int = 128, lengths: str = "log-uniform"):
+def run_serving(seconds: float, device: int, rate: float = 200.0, chunk: int = 128, lengths: str = "log-uniform",
+                max_chunk: int = 0):
     """The serving configuration: Poisson arrivals at `rate` per second of
     DM-trial series with lengths log-uniform in 2^18..2^23 samples, zmax
     uniform in {50, 100, 200, 300}, 5% with an injected signal, admitted
@@ -185,7 +188,8 @@ def run_serving(seconds: float, device: int, rate: float = 200.0, chunk: int = 1
         zmax = int(rng.choice([50, 100, 200, 300]))
         src = sig[rng.integers(len(sig))] if rng.random() < 0.05 else pool[rng.integers(len(pool))]
         arrivals.append((t, src[:n], zmax))
-    srv = Server(hbm_budget_bytes=150e9, fftlen=8192, numharm=8, chunk_segments=chunk, device=device)
+    srv = Server(hbm_budget_bytes=150e9, fftlen=8192, numharm=8, chunk_segments=chunk, device=device,
+                 max_chunk_segments=max_chunk)
     for z in (50, 100, 200, 300):  # build the four banks outside the measurement
         srv.wait(srv.submit(pool[0][: 1 << 18], DT, z), -1)
     base = srv.stats()
@@ -236,6 +240,7 @@ def run_serving(seconds: float, device: int, rate: float = 200.0, chunk: int = 1
             "groups": st["groups"] - base["groups"],
             "segments_per_group": (st["group_segments"] - base["group_segments"]) / max(1, st["groups"] - base["groups"]),
             "wall_s": wall, "hbm_budget_bytes": 150e9, "max_wait_s": 1.0, "chunk_segments": chunk,
+            "max_chunk_segments": max_chunk,
             "lengths": lengths,
             "by_length": classes,
             "workload": "Poisson arrivals, lengths log-uniform 2^18..2^23 (rounded up to even "
@@ -716,11 +721,12 @@ def run_ours(args):
         finally:
             cpu.close()
     dedisp = run_dedisperse(local) if args.serving_seconds > 0 else None
-    serving = (run_serving(args.serving_seconds, local, chunk=args.serving_chunk, lengths=args.serving_lengths)
+    serving = (run_serving(args.serving_seconds, local, chunk=args.serving_chunk, lengths=args.serving_lengths,
+                           max_chunk=args.serving_max_chunk)
                if args.serving_seconds > 0 else None)
     # the same stream at half the rate: latency when the GPU is not saturated
     serving_half = (run_serving(args.serving_seconds, local, rate=100.0, chunk=args.serving_chunk,
-                                lengths=args.serving_lengths)
+                                lengths=args.serving_lengths, max_chunk=args.serving_max_chunk)
                     if args.serving_seconds > 0 else None)
     precision = precision_report(args.precision_seeds, local) if args.precision_seeds > 0 else None
     line = {

@@ -213,7 +213,7 @@ accel_ctx* group_ctx(accel_server* s, int zmax, int* rc) {
     cfg.numharm = s->cfg.numharm;
     cfg.fftlen = s->cfg.fftlen;
     cfg.sigma = s->cfg.sigma;
-    cfg.chunk_segments = s->cfg.chunk_segments;
+    cfg.chunk_segments = std::max(s->cfg.chunk_segments, s->cfg.max_chunk_segments);
     cfg.device = s->cfg.device;
     *rc = accel_create(&cfg, &g.ctx);
     if (*rc) {
@@ -317,7 +317,16 @@ Flight launch_group(accel_server* s, int zmax, bool late_first) {
     if (!c || g.active.empty()) return f;
     f.b = g.next_buf;
     GroupBuf& B = g.buf[f.b];
-    const int cap = c->chunk;
+    // group size: chunk_segments, or with max_chunk_segments a third of the
+    // bank's prepared backlog (three groups are kept in flight) within
+    // [chunk_segments, max_chunk_segments]
+    int cap = std::min(s->cfg.chunk_segments, c->chunk);
+    if (s->cfg.max_chunk_segments > cap) {
+        long long backlog = 0;
+        for (Request* r : g.active)
+            if (r->prepared) backlog += r->nsteps - r->next_step;
+        cap = (int)std::max<long long>(cap, std::min<long long>(backlog / kFlightDepth, c->chunk));
+    }
     const long long half = (unsigned short)(c->uselen / 2);
     std::vector<Request*> order(g.active);
     const auto now = Clock::now();

@@ -45,7 +45,8 @@ class Candidate(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("fftlen", C.c_int),
                 ("numharm", C.c_int), ("sigma", C.c_double), ("chunk_segments", C.c_int),
-                ("device", C.c_int), ("max_wait_s", C.c_double), ("reserved", C.c_int * 6)]
+                ("device", C.c_int), ("max_wait_s", C.c_double), ("max_chunk_segments", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class ServerStats(C.Structure):

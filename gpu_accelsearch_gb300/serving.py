@@ -12,13 +12,14 @@ from .search import CAND_DTYPE
 
 class Server:
     def __init__(self, hbm_budget_bytes=150e9, max_active=0, fftlen=8192, numharm=8, sigma=6.0,
-                 chunk_segments=128, device=0, max_wait_s=1.0):
+                 chunk_segments=128, device=0, max_wait_s=1.0, max_chunk_segments=0):
         L = N.lib()
         cfg = N.ServerConfig()
         L.accel_server_config_init(C.byref(cfg))
         cfg.hbm_budget_bytes, cfg.max_active, cfg.fftlen = hbm_budget_bytes, max_active, fftlen
         cfg.numharm, cfg.sigma, cfg.chunk_segments, cfg.device = numharm, sigma, chunk_segments, device
         cfg.max_wait_s = max_wait_s
+        cfg.max_chunk_segments = max_chunk_segments
         h = C.c_void_p()
         N.check(L.accel_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -335,7 +335,11 @@ typedef struct accel_server_config {
     double max_wait_s;        /* requests waiting longer than this since their */
                               /* submission get every other launch group,     */
                               /* oldest first (0: 1.0 s)                       */
-    int reserved[6];
+    int max_chunk_segments;   /* > chunk_segments: a launch group grows with   */
+                              /* its bank's backlog of prepared steps (a third */
+                              /* of it, as groups are kept three deep) up to   */
+                              /* this many steps; 0: groups of chunk_segments  */
+    int reserved[5];
 } accel_server_config;
 
 typedef struct accel_server_stats {
