@@ -90,9 +90,12 @@ def test_continuous_batching_short_request_overtakes():
     assert st["groups"] > 0 and st["group_segments"] >= st["groups"] and st["prep_gpu_ms"] > 0
 
 
-def test_many_lengths_and_banks_equal_context_path():
-    # every request a new series length (a new cuFFT plan from the planner
-    # threads, the shared work area growing), two banks, submitted at once
+@pytest.mark.parametrize("max_chunk", [0, 64])
+def test_many_lengths_and_banks_equal_context_path(max_chunk):
+    # every request a new series length (odd factors of every size: the
+    # transform's power-of-two, Cooley-Tukey and Bluestein forms), two
+    # banks, submitted at once; with max_chunk the launch groups grow with
+    # the backlog (16 to 64 segments)
     from gpu_accelsearch_gb300.search import AccelSearch
     from gpu_accelsearch_gb300.serving import Server
     rng = np.random.default_rng(77)
@@ -101,7 +104,8 @@ def test_many_lengths_and_banks_equal_context_path():
         n = 2 * int(rng.integers(1 << 14, 1 << 16))
         z = 50 if i % 3 else 100
         reqs.append((synth_series(n, seed=300 + i, signals=[(0.1, 0.2 * n + 0.25, 8.0)]), z))
-    with Server(hbm_budget_bytes=4e9, fftlen=2048, numharm=4, chunk_segments=16) as srv:
+    with Server(hbm_budget_bytes=4e9, fftlen=2048, numharm=4, chunk_segments=16,
+                max_chunk_segments=max_chunk) as srv:
         ids = [srv.submit(x, DT, z) for x, z in reqs]
         for i in ids:
             assert srv.wait(i, 120)
