@@ -57,6 +57,9 @@ def parse():
                     help="segment length; 0: chosen by the autotuner among 4096/8192/16384")
     ap.add_argument("--split", type=int, default=-1, help="plane kernel layout (-1: autotuner)")
     ap.add_argument("--tuning", default="", help="JSON of extra accel_tuning fields to apply")
+    ap.add_argument("--short-transforms", type=int, default=-1, choices=[-1, 0, 1],
+                    help="1: short (R*2^k) segment transforms, 0: the reference's powers of two, "
+                         "-1: the library default")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -516,16 +519,18 @@ def run_ours(args):
     ptrs = [x.data_ptr() for x in series]
     from gpu_accelsearch_gb300.search import autotune
     tuned = None
+    short = None if args.short_transforms < 0 else bool(args.short_transforms)
     if args.fftlen == 0 or args.chunk == 0 or args.split < 0:
         fl = (4096, 8192, 16384) if args.fftlen == 0 else (args.fftlen,)
-        kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=1100, device=local)
+        kw, tun, rate = autotune(ZMAX, NUMHARM, fftlens=fl, steps=1100, device=local, short_transforms=short)
         tuned = {"fftlen": kw["fftlen"], "chunk_segments": tun["chunk_segments"],
                  "plane_split": tun["plane_split"], "fused_sum": tun["fused_sum"],
                  "hsum_tile_rows": tun["hsum_tile_rows"], "sample_cells_per_s": rate}
     fftlen = args.fftlen or tuned["fftlen"]
     chunk = args.chunk or tuned["chunk_segments"]
     split = args.split if args.split >= 0 else tuned["plane_split"]
-    s = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local)
+    s = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local,
+                    short_transforms=short)
     extra = json.loads(args.tuning) if args.tuning else {}
     if tuned and "fused_sum" not in extra:
         extra["fused_sum"] = tuned["fused_sum"]
@@ -620,7 +625,8 @@ def run_ours(args):
             n1 = search.step_count(1 << 22, DT)
             return n1, n1 * search.uselen * search.harmonics[0].numzs * reps / (search.stats()["search_ms"] / 1e3)
 
-        p = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=1, device=local)
+        p = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=FFTLEN, chunk_segments=1, device=local,
+                        short_transforms=short)
         pn, pv = time_trial(p)
         p.close()
         plain = {"value": pv, "unit": "cells/s",
@@ -628,7 +634,8 @@ def run_ours(args):
                              f"({pn} steps, L={FFTLEN}): the reference's step-at-a-time control flow"}
         # the batch itself, one trial per search call (device-resident
         # series, the batched search's tuned launch shape)
-        q = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local)
+        q = AccelSearch(zmax=ZMAX, numharm=NUMHARM, fftlen=fftlen, chunk_segments=chunk, device=local,
+                        short_transforms=short)
         q.set_tuning(chunk_segments=chunk, plane_split=split, **extra)
         for i in range(min(4, len(ptrs))):
             q.search([ptrs[i]], DT, on_device=True, nsamples=[lengths[i]])
@@ -742,6 +749,7 @@ def run_ours(args):
                                f"L={fftlen} (uselen {U}) chosen by the autotuner, sigma=6",
                    "segments_per_step": nseg, "cells_per_step": cells,
                    "fftlen": fftlen, "uselen": U, "tuning": s.tuning(), "autotuner": tuned,
+                   "transform_lengths": [h.fftlen for h in s.harmonics],
                    "l2": f"inputs ({sum(lengths) * 4 / 1e9:.2f} GB of series per GPU) larger "
                          "than L2; no flush",
                    "parallelism": f"trial-sharded replicas x{world}"},

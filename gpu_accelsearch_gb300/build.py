@@ -26,11 +26,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "bank.cu", "search.cu", "search_plane_lo.cu", "search_plane_hi.cu",
            "search_fund_lo.cu", "search_fund_hi.cu", "tune.cu", "whiten.cu", "compat.cu",
            "server.cu", "sift.cu", "optimize.cu", "dedisperse.cu",
-           "filterbank.cu", "compat_cxx.cu", "search_step.cu", "rfft.cu"]
+           "filterbank.cu", "compat_cxx.cu", "search_step.cu", "rfft.cu", "search_mixed5.cu",
+           "search_mixed6.cu", "search_mixed7.cu", "search_mixed_prep.cu"]
 EXTRA = {"bank.cu": ["-fmad=false"], "compat.cu": ["-Xcompiler", "-ffp-contract=off"],
          "dedisperse.cu": ["-Xcompiler", "-ffp-contract=off"]}
 HEADERS = ["accel_common.cuh", "accel_internal.h", "context.h", "fft_smem.cuh", "search_kernels.cuh",
-           "step_kernel.cuh"]
+           "step_kernel.cuh", "fft_mixed.cuh", "mixed_kernels.cuh"]
 
 
 def nvcc() -> str:

@@ -45,6 +45,49 @@ constexpr int kTwTotal = kTwN + kTwPacked;
 constexpr int kMinM = 64;           // smallest half-length FFT
 constexpr int kMaxM = 8192;         // largest half-length FFT (L <= 16384)
 
+// Short transforms: besides powers of two, the plane kernels take half
+// lengths M = R * N2 with R = 5, 6 or 7 and N2 a power of two in
+// [kMixedMinN2, kMixedMaxN2].  Such a transform is R transforms of N2
+// points and one radix-R pass; its segment spectra and folded templates are
+// stored in decimated order: position (k mod R) * N2 + k / R holds point k.
+constexpr int kMixedMinN2 = 64;
+constexpr int kMixedMaxN2 = 512;
+// Behind the tables above, the twiddles of the radix-R pass of every short
+// length, R = 5, 6, 7 and N2 = 64 .. 512 in turn: (R - 1) * N2 entries,
+// entry (g - 1) * N2 + b = exp(2 pi i g b / (R N2)), so that the threads of
+// consecutive butterflies b load consecutive addresses.
+ACCEL_HD constexpr int tw_form_off(int R, int N2) {
+    int off = kTwTotal;
+    for (int r = 5; r <= 7; r++)
+        for (int n = kMixedMinN2; n <= kMixedMaxN2; n *= 2) {
+            if (r == R && n == N2) return off;
+            off += (r - 1) * n;
+        }
+    return off;
+}
+constexpr int kTwAll = tw_form_off(8, 0);  // the end of the last section
+
+// R of a plane-kernel half length M: 1 for a power of two, R for R * N2 as
+// above, 0 for anything else.
+ACCEL_HD int mixed_radix(int M) {
+    if (M <= 0) return 0;
+    if ((M & (M - 1)) == 0) return 1;
+    for (int R = 5; R <= 7; R++) {
+        if (M % R) continue;
+        const int n2 = M / R;
+        if ((n2 & (n2 - 1)) == 0 && n2 >= kMixedMinN2 && n2 <= kMixedMaxN2) return R;
+    }
+    return 0;
+}
+
+// Storage position of point k of a half length M transform (identity for a
+// power of two).
+ACCEL_HD int decimated_pos(int k, int M, int R) {
+    if (R <= 1) return k;
+    const int n2 = M / R;
+    return (k % R) * n2 + k / R;
+}
+
 // ---------------------------------------------------------------- geometry
 // z_response_halfwidth (bpd_subharmonics.cu:31-45) -- double arithmetic on
 // purpose: the truncation points must match the reference.

@@ -163,6 +163,23 @@ void prof_collect(accel_ctx* c) {
     c->pending.clear();
 }
 
+// Shortest half length of a plane-kernel transform (a power of two, or
+// R * N2 with R = 5, 6, 7: accel_common.cuh) that holds the harmonic's
+// segment of numdata bins at every step phase (the geometry repeats with
+// period q in startr); M (the reference's power of two) if none is shorter.
+// The powers kept, columns [hw0, hw0 + numrs/2) of the even and odd
+// outputs, are a linear correlation of the first numdata bins with
+// templates of halfwidth <= hw0, which any length >= numdata gives.
+int short_half_length(int M, int U, int p, int q, int hw0) {
+    int need = 0;
+    for (long long s = 0; s < 4LL * q; s++) need = std::max(need, step_harm(1000000 + s, U, p, q, hw0).numdata);
+    int best = M;
+    for (int R = 5; R <= 7; R++)
+        for (int n2 = kMixedMinN2; n2 <= kMixedMaxN2; n2 *= 2)
+            if (R * n2 >= need && R * n2 < best && mixed_radix(R * n2) == R) best = R * n2;
+    return best;
+}
+
 int build_bank(accel_ctx* c) {
     int info_zmax = c->cfg.zmax, numharm = c->cfg.numharm, U = c->uselen;
     // bank order: stage by stage, odd harmonics (bpd_subharmonics.cu:319-354)
@@ -188,6 +205,9 @@ int build_bank(accel_ctx* c) {
             b.M = (int)(L / 2);
             b.hw0 = z_halfwidth((double)(-b.zmax));
             b.zlo = required_z(h, maxh, -info_zmax);
+            // (the fundamental keeps its power of two: the fused sum's kernel
+            // takes powers of two only)
+            if (c->cfg.short_transforms && n > 0) b.M = short_half_length(b.M, U, h, maxh, b.hw0);
             b.tpl_base = tb;
             tb += b.numzs;
             int hwmax = b.hw0;
@@ -255,7 +275,8 @@ int build_plan(accel_ctx* c) {
         for (long long s = 0; s < 4LL * P.q; s++) {
             StepHarm g = step_harm(1000000 + s, U, P.p, P.q, P.hw0);
             wmax = std::max(wmax, g.numrs);
-            if (next_pow2(g.numdata) != P.M)
+            const bool fits = c->cfg.short_transforms ? g.numdata <= P.M : next_pow2(g.numdata) == P.M;
+            if (!fits || mixed_radix(P.M) == 0)
                 return set_err(ACCEL_ERR_INVALID,
                                "harmonic %d/%d: segment of %d bins does not fit half length %d", P.p,
                                P.q, g.numdata, P.M);
@@ -288,6 +309,9 @@ int build_plan(accel_ctx* c) {
     for (int h = 0; h < c->nh; h++)
         if (std::find(c->mvals.begin(), c->mvals.end(), c->hp[h].M) == c->mvals.end())
             c->mvals.push_back(c->hp[h].M);
+    // power-of-two classes first: the short ones share one preparation launch
+    // issued after them
+    std::stable_partition(c->mvals.begin(), c->mvals.end(), [](int M) { return mixed_radix(M) == 1; });
     for (int s = 0; s < c->nstages; s++)
         c->cuts[s] = (float)power_cut(c->cfg.sigma, 1 << s, c->cfg.numindep);
     // Largest shared-memory footprint of a k_hsum_tile tile of each height,
@@ -512,7 +536,27 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
     if (!sum_stream) sum_stream = c->stream;
     float2* dbuf = dh_in ? const_cast<float2*>(dh_in) : c->dbuf;
     float* planes = planes_out ? planes_out : c->planes;
+    bool short_prepped = !do_prep;
     for (int M : c->mvals) {
+        if (mixed_radix(M) > 1 && !short_prepped) {
+            // the segments of every short-transform harmonic in one launch,
+            // after the power-of-two classes' planes (the fundamental's
+            // first): by then the previous group's harmonic sum on the other
+            // stream has usually left the SMs
+            short_prepped = true;
+            PrepArgs ps{};
+            int k = 0;
+            for (int h = 0; h < c->nh; h++)
+                if (mixed_radix(c->hp[h].M) > 1) ps.h[k++] = c->hp[h];
+            ps.nh = k;
+            ps.uselen = c->uselen;
+            ps.exact_rsqrt = c->cfg.exact_rsqrt;
+            ps.segs = d_segs;
+            ps.dbuf = dbuf;
+            ps.dstride = c->dstride;
+            ProfScope pscope(c, K_PREP, 1);
+            CKL(launch_prep(M, ps, nseg, c->tw, c->stream), "segment preparation");
+        }
         PrepArgs pa{};
         PlaneArgs la{};
         int k = 0, kp = 0, zb = 0;
@@ -539,7 +583,7 @@ int run_group(accel_ctx* c, const SegDesc* d_segs, int nseg, int seg_base, float
         la.pstride = c->pstride;
         la.use_fp16 = c->cfg.template_fp16;
         la.split = c->plane_split;
-        if (do_prep) {
+        if (do_prep && mixed_radix(M) == 1) {
             ProfScope ps(c, K_PREP, 1);
             CKL(launch_prep(M, pa, nseg, c->tw, c->stream), "segment preparation");
         }
@@ -1084,7 +1128,7 @@ int accel_create(const accel_config* cfg, accel_ctx** out) {
         c->own_stream = true;
     }
     if (!rc) {
-        cudaError_t e = cudaMalloc(&c->tw, sizeof(float2) * kTwTotal);
+        cudaError_t e = cudaMalloc(&c->tw, sizeof(float2) * kTwAll);
         if (e != cudaSuccess) rc = set_err(ACCEL_ERR_NOMEM, "twiddles: %s", cudaGetErrorString(e));
         else if (launch_twiddles(c->tw, c->stream) != 0) rc = set_err(ACCEL_ERR_CUDA, "twiddle launch");
     }
@@ -1506,7 +1550,7 @@ int accel_bank_spectra(const accel_ctx* c, int h, accel_complex* kstd, accel_com
     CK(cudaSetDevice(c->device));
     if (kstd) CK(cudaMemcpy(kstd, b.kstd, sizeof(float2) * n, cudaMemcpyDeviceToHost));
     if (fold) {
-        // the device copy is scaled by 1/L (exact); A and B are returned unscaled
+        // the device copy is scaled by 1/L; A and B are returned unscaled
         CK(cudaMemcpy(fold, b.fold, sizeof(float2) * n, cudaMemcpyDeviceToHost));
         const float L = 2.0f * (float)b.M;
         for (size_t i = 0; i < n; i++) {

@@ -202,14 +202,16 @@ __global__ void k_template_dft(const BankHarmDev* __restrict__ hd, int nh, const
     float2* kstd = H.kstd + (size_t)j * L;
     kstd[k] = make_float2((float)(ser + sor), (float)(sei + soi));
     kstd[k + H.M] = make_float2((float)(ser - sor), (float)(sei - soi));
-    // folded spectra scaled by 1/L (a power of two: exact), so that the
-    // plane kernels' |y|^2 is already the normalised power |y / L|^2
+    // folded spectra scaled by 1/L (exact for a power of two), so that the
+    // plane kernels' |y|^2 is already the normalised power |y / L|^2; a
+    // short transform's fold is stored in decimated order
     const double inv_l = 1.0 / L;
     float2* fold = H.fold + (size_t)j * 2 * H.M;
-    fold[k] = make_float2((float)(2.0 * ser * inv_l), (float)(-2.0 * sei * inv_l));
+    const int pk = decimated_pos(k, H.M, mixed_radix(H.M));
+    fold[pk] = make_float2((float)(2.0 * ser * inv_l), (float)(-2.0 * sei * inv_l));
     // So * w, then conjugate, times 2
     double qr = sor * cw - soi * sw, qi = sor * sw + soi * cw;
-    fold[H.M + k] = make_float2((float)(2.0 * qr * inv_l), (float)(-2.0 * qi * inv_l));
+    fold[H.M + pk] = make_float2((float)(2.0 * qr * inv_l), (float)(-2.0 * qi * inv_l));
 }
 
 // FP16 copy of the folded bank, scaled per template by its largest
@@ -247,10 +249,22 @@ __global__ void k_fold_to_half(const BankHarmDev* __restrict__ hd, int nh) {
 }
 
 // Entry i of the twiddle buffer: the table W^m (m < kTwN), then the packed
-// per-pass sections (accel_common.cuh), each a copy of table entry m.
+// per-pass sections (accel_common.cuh), each a copy of table entry m, then
+// the radix-R sections of the short transforms.
 __global__ void k_twiddles(float2* tw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kTwTotal) return;
+    if (i >= kTwAll) return;
+    if (i >= kTwTotal) {  // the radix-R sections: exp(2 pi i g b / (R N2))
+        int R = 5, n2 = kMixedMinN2;
+        for (int r = 5; r <= 7; r++)
+            for (int n = kMixedMinN2; n <= kMixedMaxN2; n *= 2)
+                if (i >= tw_form_off(r, n)) R = r, n2 = n;
+        const int j = i - tw_form_off(R, n2), g = j / n2 + 1, b = j % n2;
+        double s, c;
+        sincospi(2.0 * (double)(g * b) / (double)(R * n2), &s, &c);
+        tw[i] = make_float2((float)c, (float)s);
+        return;
+    }
     int m = i;
     if (i >= kTwN + kTwFull256) {
         const int q = i - kTwN - kTwFull256, j = q / 16 + 1, k = q % 16;
@@ -270,7 +284,7 @@ __global__ void k_twiddles(float2* tw) {
 }
 
 int launch_twiddles(float2* tw, cudaStream_t st) {
-    k_twiddles<<<(kTwTotal + 255) / 256, 256, 0, st>>>(tw);
+    k_twiddles<<<(kTwAll + 255) / 256, 256, 0, st>>>(tw);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -58,7 +58,7 @@ bool ensure_twiddles() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     if (g_cs.tw && g_cs.tw_device == dev) return true;
-    if (cudaMalloc(&g_cs.tw, sizeof(float2) * kTwTotal) != cudaSuccess) return false;
+    if (cudaMalloc(&g_cs.tw, sizeof(float2) * kTwAll) != cudaSuccess) return false;
     if (launch_twiddles(g_cs.tw, 0) != 0) return false;
     g_cs.tw_device = dev;
     return cudaStreamSynchronize(0) == cudaSuccess;

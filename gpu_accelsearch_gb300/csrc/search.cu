@@ -5,7 +5,13 @@
 
 namespace accel {
 
+int launch_prep_short(const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st);
+int launch_plane_r5(int N2, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
+int launch_plane_r6(int N2, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
+int launch_plane_r7(int N2, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st);
+
 int launch_prep(int M, const PrepArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    if (mixed_radix(M) > 1) return launch_prep_short(a, nseg, tw, st);  // any short harmonics
     switch (M) {
         case 64: return prep_m<64>(a, nseg, tw, st);
         case 128: return prep_m<128>(a, nseg, tw, st);
@@ -128,6 +134,11 @@ int launch_fund_sum_lo(const FundArgs& a, int nseg, const float2* tw, cudaStream
 int launch_fund_sum_hi(const FundArgs& a, int nseg, const float2* tw, cudaStream_t st);
 
 int launch_plane(int M, const PlaneArgs& a, int nseg, const float2* tw, cudaStream_t st) {
+    switch (mixed_radix(M)) {  // short transforms
+        case 5: return launch_plane_r5(M / 5, a, nseg, tw, st);
+        case 6: return launch_plane_r6(M / 6, a, nseg, tw, st);
+        case 7: return launch_plane_r7(M / 7, a, nseg, tw, st);
+    }
     return M >= 2048 ? launch_plane_hi(M, a, nseg, tw, st) : launch_plane_lo(M, a, nseg, tw, st);
 }
 

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(M / 16) k_prep(const PrepArgs a, const float2*
     const SegDesc sd = a.segs[blockIdx.y];
     const StepHarm g = step_harm(sd.startr, a.uselen, H.p, H.q, H.hw0);
     const int t = threadIdx.x;
-    const int numdata = g.numdata < M ? g.numdata : M;  // host checks next_pow2(numdata) == M
+    const int numdata = g.numdata < M ? g.numdata : M;  // host checks numdata <= M
 
     float2 x[1][16];
 #pragma unroll

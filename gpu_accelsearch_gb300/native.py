@@ -28,7 +28,8 @@ class Config(C.Structure):
                 ("uselen", C.c_int), ("whiten_initbuf", C.c_int), ("whiten_maxbuf", C.c_int),
                 ("sigma", C.c_double), ("numindep", C.c_double), ("template_fp16", C.c_int),
                 ("chunk_segments", C.c_int), ("cand_capacity", C.c_longlong),
-                ("device", C.c_int), ("exact_rsqrt", C.c_int), ("reserved", C.c_int * 6)]
+                ("device", C.c_int), ("exact_rsqrt", C.c_int), ("short_transforms", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class Harmonic(C.Structure):

@@ -100,19 +100,21 @@ def first_bin(nsamples: int, dt: float) -> int:
 
 
 def autotune(zmax=200, numharm=8, fftlens=(4096, 8192, 16384), steps=64, template_fp16=False,
-             device=0):
+             device=0, short_transforms=None):
     """Pick the segment length and launch shape by timing them on this GPU.
     Returns (kwargs for AccelSearch, tuning dict, cells/s)."""
     L = N.lib()
     base = N.Config()
     L.accel_config_init(C.byref(base))
     base.zmax, base.numharm, base.template_fp16, base.device = zmax, numharm, int(template_fp16), device
+    if short_transforms is not None:
+        base.short_transforms = int(bool(short_transforms))
     fl = (C.c_int * len(fftlens))(*fftlens)
     best, tun, rate = N.Config(), N.Tuning(), C.c_double()
     N.check(L.accel_autotune(C.byref(base), fl, len(fftlens), steps, C.byref(best), C.byref(tun),
                              C.byref(rate)))
     kw = dict(zmax=zmax, numharm=numharm, fftlen=best.fftlen, template_fp16=template_fp16,
-              chunk_segments=best.chunk_segments, device=device)
+              chunk_segments=best.chunk_segments, device=device, short_transforms=bool(best.short_transforms))
     return kw, {"chunk_segments": tun.chunk_segments, "plane_split": tun.plane_split,
                 "fused_sum": tun.fused_sum, "hsum_tile_rows": tun.hsum_tile_rows or 16}, rate.value
 
@@ -120,7 +122,7 @@ def autotune(zmax=200, numharm=8, fftlens=(4096, 8192, 16384), steps=64, templat
 class AccelSearch:
     def __init__(self, zmax=200, numharm=8, fftlen=8192, uselen=0, sigma=6.0, numindep=1.0,
                  whiten_initbuf=6, whiten_maxbuf=200, template_fp16=False, chunk_segments=0,
-                 cand_capacity=0, device=0, exact_rsqrt=False):
+                 cand_capacity=0, device=0, exact_rsqrt=False, short_transforms=None):
         L = N.lib()
         cfg = N.Config()
         L.accel_config_init(C.byref(cfg))
@@ -130,9 +132,12 @@ class AccelSearch:
         cfg.template_fp16 = int(bool(template_fp16))
         cfg.chunk_segments, cfg.cand_capacity, cfg.device = chunk_segments, cand_capacity, device
         cfg.exact_rsqrt = int(bool(exact_rsqrt))
+        if short_transforms is not None:  # None: the library's default
+            cfg.short_transforms = int(bool(short_transforms))
         self.config = cfg
         self.kwargs = dict(zmax=zmax, numharm=numharm, fftlen=fftlen, template_fp16=template_fp16,
-                           chunk_segments=chunk_segments, device=device)
+                           chunk_segments=chunk_segments, device=device,
+                           short_transforms=bool(cfg.short_transforms))
         h = C.c_void_p()
         N.check(L.accel_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -52,13 +52,23 @@ typedef struct accel_config {
     int exact_rsqrt;        /* 1: whitening and segment normalisation use an IEEE */
                             /* 1/sqrt instead of the reference's magic-constant  */
                             /* approximation (bpd_math.c:94-105; ~1.75e-3 error) */
-    int reserved[6];
+    int short_transforms;   /* 1: each harmonic's segment transform has the      */
+                            /* shortest length R*2^k (R = 1, 5, 6, 7) that holds */
+                            /* its data instead of the reference's power of two  */
+                            /* (bpd_subharmonics.cu:60-67); the powers kept are   */
+                            /* the same up to FP32 rounding.  Such a harmonic's  */
+                            /* segment spectra (accel_prepare_segments) and      */
+                            /* folded templates (accel_bank_spectra) are stored  */
+                            /* in decimated order: position (k mod R)*(M/R)+k/R  */
+                            /* holds point k (M = fftlen/2 of accel_harmonic)    */
+    int reserved[5];
 } accel_config;
 
 typedef struct accel_harmonic {
     int harmnum, maxharm;   /* harmonic fraction harmnum/maxharm                 */
     int zmax, numzs;        /* templates z = -zmax .. zmax step 2                */
-    int fftlen;             /* segment length L_h                                */
+    int fftlen;             /* segment length L_h transformed (short_transforms: */
+                            /* may be R*2^k instead of the reference's 2^k)     */
     int halfwidth;          /* halfwidth of the widest template (binOffset)      */
     int zlo;                /* lowest f-dot of the harmonic's plane              */
     int plane_width;        /* powers per f-dot row kept on the device           */

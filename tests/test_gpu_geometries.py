@@ -31,11 +31,17 @@ def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a).view(np.float32).copy()).cuda()
 
 
-@pytest.fixture(scope="module", params=GEOMS, ids=lambda g: "z%d_h%d_L%d" % g)
+# every geometry with the reference's power-of-two transforms and with the
+# short transforms (R * 2^k points, R = 5, 6, 7: the 3/4, 5/8, 7/8, 1/4, 3/8
+# and 1/8 harmonics at zmax 200)
+@pytest.fixture(scope="module", params=[g + (sh,) for sh in (False, True) for g in GEOMS],
+                ids=lambda g: "z%d_h%d_L%d" % g[:3] + ("_short" if g[3] else ""))
 def G(request):
     from gpu_accelsearch_gb300.search import AccelSearch
-    zmax, nh, L = request.param
-    s = AccelSearch(zmax=zmax, numharm=nh, fftlen=L)
+    zmax, nh, L, short = request.param
+    s = AccelSearch(zmax=zmax, numharm=nh, fftlen=L, short_transforms=short)
+    if short:  # some harmonic really runs a short transform
+        assert any(h.fftlen & (h.fftlen - 1) for h in s.harmonics), s.harmonics
     U = s.uselen
     n = 1 << 20
     # one accelerated signal in the middle of step SIG_STEP's fundamental range
