@@ -13,8 +13,9 @@
 //
 // Both kernels do exactly what k_prep and k_plane do (the same median
 // normalisation, products, powers and stores), on the decimated storage
-// order of the segment spectra and folded templates.  Instantiations live in
-// search_mixed{5,6,7}.cu.
+// order of the segment spectra and folded templates.  The plane kernels are
+// instantiated in search_mixed{5,6,7}.cu, the preparation kernel (one for
+// every short length) in search_mixed_prep.cu.
 #pragma once
 
 #include "fft_mixed.cuh"
